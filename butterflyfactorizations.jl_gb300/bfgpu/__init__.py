@@ -1,0 +1,356 @@
+"""bfgpu -- Python host mirror of the ButterflyFactorizations.jl far-field interface.
+
+The functions mirror the reference's operator interface on top of the C ABI of
+``libbfgpu.so``:
+
+=====================================  =============================================
+reference (Julia)                      here
+=====================================  =============================================
+``assemble_BF(km, blktree, no, ns,     ``assemble_BF(obs, src, tree_o, tree_s, no,
+k, tau; ...)`` (bfassembly.jl:48)      ns, k, tau, ...)`` -> ``Operator``
+``PetrovGalerkinBF(op, X, Y, tree,     ``PetrovGalerkinBF(obs, src, tree_o, tree_s, k,
+k; tol, ...)`` far part                 tol=1e-3, ...)`` -> ``Operator``
+(petrovgalerkinbf.jl:33)
+``mul!(y, A, x, alpha, beta)``         ``mul(y, A, x, alpha, beta)``
+(matrixvector.jl:8)
+``A * x``                              ``A @ x``
+``adjoint(A)``, ``transpose(A)``       ``A.adjoint()``, ``A.transpose()`` (lazy; no copy)
+``size(A)``                            ``A.shape``
+``nearandfar(tree, alpha)``            ``nearandfar(tree_o, tree_s, alpha)``
+=====================================  =============================================
+
+All compute runs in ``libbfgpu.so`` on the GPU; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import (BF_OP_C, BF_OP_N, BF_OP_T, BF_PTR_DEVICE, BF_PTR_HOST, BFError, BuildOpts,
+                   FactorDesc, OpStats, check, load)
+
+__all__ = ["Tree", "Context", "Operator", "nearandfar", "assemble_BF", "PetrovGalerkinBF",
+           "import_blocks", "mul", "BFError", "load"]
+
+
+def _p(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+class Tree:
+    """2^3 cluster tree built by the library (``bf_tree_build``)."""
+
+    def __init__(self, handle, points=None):
+        self._h = C.c_void_p(handle)
+        self.points = points
+        lib = load()
+        nn, npnt, depth = C.c_int64(), C.c_int64(), C.c_int32()
+        check(lib.bf_tree_size(self._h, C.byref(nn), C.byref(npnt), C.byref(depth)), "tree_size")
+        n, m = nn.value, npnt.value
+        self.center = np.zeros((n, 3))
+        self.halfsize = np.zeros(n)
+        self.level = np.zeros(n, np.int32)
+        self.parent = np.zeros(n, np.int32)
+        self.first_child = np.zeros(n, np.int32)
+        self.n_child = np.zeros(n, np.int32)
+        self.begin = np.zeros(n, np.int64)
+        self.end = np.zeros(n, np.int64)
+        self.perm = np.zeros(m, np.int64)
+        check(lib.bf_tree_export(self._h, _p(self.center, C.c_double), _p(self.halfsize, C.c_double),
+                                 _p(self.level, C.c_int32), _p(self.parent, C.c_int32),
+                                 _p(self.first_child, C.c_int32), _p(self.n_child, C.c_int32),
+                                 _p(self.begin, C.c_int64), _p(self.end, C.c_int64),
+                                 _p(self.perm, C.c_int64)), "tree_export")
+        self.depth = depth.value
+
+    @classmethod
+    def build(cls, points, max_points: int | None = None, max_depth: int | None = None):
+        lib = load()
+        pts = np.ascontiguousarray(points, dtype=np.float64)
+        h = C.c_void_p()
+        check(lib.bf_tree_build(_p(pts, C.c_double), pts.shape[0],
+                                -1 if max_points is None else int(max_points),
+                                -1 if max_depth is None else int(max_depth), C.byref(h)),
+              "bf_tree_build")
+        return cls(h.value, pts)
+
+    @property
+    def n_nodes(self):
+        return len(self.halfsize)
+
+    def values(self, node):
+        return self.perm[self.begin[node]:self.end[node]]
+
+    def children(self, node):
+        f = int(self.first_child[node])
+        return range(f, f + int(self.n_child[node]))
+
+    def isleaf(self, node):
+        return self.n_child[node] == 0
+
+    def values_csr(self):
+        """node -> values map as CSR (ptr, idx) over all nodes."""
+        lens = (self.end - self.begin).astype(np.int64)
+        ptr = np.zeros(self.n_nodes + 1, np.int64)
+        np.cumsum(lens, out=ptr[1:])
+        idx = np.concatenate([self.values(i) for i in range(self.n_nodes)]).astype(np.int64)
+        return ptr, idx
+
+    def __del__(self):
+        try:
+            if self._h and self._h.value:
+                load().bf_tree_destroy(self._h)
+        except Exception:
+            pass
+
+
+def nearandfar(tree_o: Tree, tree_s: Tree, alpha: float = 1.0, minbflvl: int = 3,
+               leafcomp: bool = True, leafimbalance: bool = True):
+    """Far pairs (n_far, 2) [observer node, source node] and the near-pair count."""
+    lib = load()
+    nf, nn = C.c_int64(), C.c_int64()
+    args = (tree_o._h, tree_s._h, float(alpha), int(minbflvl), int(leafcomp), int(leafimbalance))
+    check(lib.bf_nearandfar(*args, None, None, 0, C.byref(nf), C.byref(nn)), "bf_nearandfar")
+    fo = np.zeros(max(nf.value, 1), np.int64)
+    fs = np.zeros(max(nf.value, 1), np.int64)
+    check(lib.bf_nearandfar(*args, _p(fo, C.c_int64), _p(fs, C.c_int64), max(nf.value, 1),
+                            C.byref(nf), C.byref(nn)), "bf_nearandfar")
+    return np.stack([fo[:nf.value], fs[:nf.value]], axis=1), nn.value
+
+
+class Context:
+    """One CUDA device (``bf_ctx_create``)."""
+
+    def __init__(self, device: int = 0):
+        lib = load()
+        h = C.c_void_p()
+        check(lib.bf_ctx_create(int(device), C.byref(h)), "bf_ctx_create")
+        self._h = h
+        self.device = device
+
+    def __del__(self):
+        try:
+            if self._h and self._h.value:
+                load().bf_ctx_destroy(self._h)
+        except Exception:
+            pass
+
+
+_default_ctx = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+class Operator:
+    """Device-resident far-field butterfly operator (a LinearMap-like object)."""
+
+    def __init__(self, handle, ctx: Context, trans: int = BF_OP_N, parent=None):
+        self._h = C.c_void_p(handle) if not isinstance(handle, C.c_void_p) else handle
+        self.ctx = ctx
+        self.trans = trans
+        self._parent = parent  # keeps the owner alive for lazy adjoint views
+        lib = load()
+        r, c = C.c_int64(), C.c_int64()
+        check(lib.bf_op_size(self._h, C.byref(r), C.byref(c)), "bf_op_size")
+        self._nr, self._nc = r.value, c.value
+
+    @property
+    def shape(self):
+        return (self._nr, self._nc) if self.trans == BF_OP_N else (self._nc, self._nr)
+
+    def adjoint(self):
+        if self.trans == BF_OP_N:
+            return Operator(self._h, self.ctx, BF_OP_C, self)
+        if self.trans == BF_OP_C:
+            return Operator(self._h, self.ctx, BF_OP_N, self)
+        raise ValueError("adjoint of a transpose view is not supported")
+
+    H = property(adjoint)
+
+    def transpose(self):
+        if self.trans == BF_OP_N:
+            return Operator(self._h, self.ctx, BF_OP_T, self)
+        if self.trans == BF_OP_T:
+            return Operator(self._h, self.ctx, BF_OP_N, self)
+        raise ValueError("transpose of an adjoint view is not supported")
+
+    T = property(transpose)
+
+    def stats(self) -> dict:
+        s = OpStats()
+        check(load().bf_op_stats_get(self._h, C.byref(s)), "bf_op_stats_get")
+        return {k: getattr(s, k) for k, _ in OpStats._fields_}
+
+    def matvec(self, x, y=None, alpha=1.0, beta=0.0, mixed: bool = False):
+        """y = beta*y + alpha*op(A)*x for host complex128 arrays (n,) or (n, nrhs)."""
+        lib = load()
+        x = np.asarray(x)
+        vec = x.ndim == 1
+        X = np.asfortranarray(x.reshape(x.shape[0], -1).astype(np.complex128, copy=False))
+        nin = self.shape[1]
+        nout = self.shape[0]
+        if X.shape[0] != nin:
+            raise ValueError(f"x has {X.shape[0]} rows, operator needs {nin}")
+        nrhs = X.shape[1]
+        if y is None:
+            Y = np.zeros((nout, nrhs), dtype=np.complex128, order="F")
+            beta = 0.0
+        else:
+            Y = y.reshape(nout, -1)
+            if not (Y.dtype == np.complex128 and Y.flags.f_contiguous):
+                raise ValueError("y must be a Fortran-ordered complex128 array")
+        a = (C.c_double * 2)(complex(alpha).real, complex(alpha).imag)
+        b = (C.c_double * 2)(complex(beta).real, complex(beta).imag)
+        fn = lib.bf_matvec_mixed if mixed else lib.bf_matvec
+        check(fn(self._h, self.trans, nrhs, X.ctypes.data, X.shape[0], Y.ctypes.data, Y.shape[0],
+                 a, b, BF_PTR_HOST, None), "bf_matvec_mixed" if mixed else "bf_matvec")
+        if y is not None:
+            return y
+        return Y[:, 0] if vec else Y
+
+    def matvec_device(self, x_ptr: int, ldx: int, y_ptr: int, ldy: int, nrhs: int = 1,
+                      alpha=1.0, beta=0.0, stream: int = 0, mixed: bool = False):
+        """Stream-ordered matvec on device pointers (complex128 column-major)."""
+        lib = load()
+        a = (C.c_double * 2)(complex(alpha).real, complex(alpha).imag)
+        b = (C.c_double * 2)(complex(beta).real, complex(beta).imag)
+        fn = lib.bf_matvec_mixed if mixed else lib.bf_matvec
+        check(fn(self._h, self.trans, int(nrhs), C.c_void_p(x_ptr), int(ldx), C.c_void_p(y_ptr),
+                 int(ldy), a, b, BF_PTR_DEVICE, C.c_void_p(stream) if stream else None),
+              "bf_matvec(device)")
+
+    def __matmul__(self, x):
+        return self.matvec(x)
+
+    def export_blocks(self):
+        """Factors as reference-style block arrays (see ``bf_op_export_blocks``)."""
+        lib = load()
+        nb, nd = C.c_int64(), C.c_int64()
+        N = None
+        check(lib.bf_op_export_blocks(self._h, C.byref(nb), C.byref(nd), *([N] * 11)), "export")
+        n = nb.value
+        out = dict(bf=np.zeros(n, np.int32), stage=np.zeros(n, np.int32),
+                   obs_out=np.zeros(n, np.int64), src_out=np.zeros(n, np.int64),
+                   obs_in=np.zeros(n, np.int64), src_in=np.zeros(n, np.int64),
+                   rows=np.zeros(n, np.int32), cols=np.zeros(n, np.int32),
+                   identity=np.zeros(n, np.int8), data_off=np.zeros(n, np.int64),
+                   data=np.zeros(max(nd.value, 1), np.complex128))
+        check(lib.bf_op_export_blocks(
+            self._h, C.byref(nb), C.byref(nd), _p(out["bf"], C.c_int32), _p(out["stage"], C.c_int32),
+            _p(out["obs_out"], C.c_int64), _p(out["src_out"], C.c_int64),
+            _p(out["obs_in"], C.c_int64), _p(out["src_in"], C.c_int64),
+            _p(out["rows"], C.c_int32), _p(out["cols"], C.c_int32), _p(out["identity"], C.c_int8),
+            _p(out["data_off"], C.c_int64), out["data"].ctypes.data_as(C.POINTER(C.c_double))),
+            "export")
+        return out
+
+    def close(self):
+        if self._parent is None and self._h and self._h.value:
+            load().bf_op_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def mul(y, A: Operator, x, alpha=1.0, beta=0.0):
+    """``mul!(y, A, x, alpha, beta)``: y <- beta*y + alpha*A*x (in place, returns y)."""
+    return A.matvec(x, y=y, alpha=alpha, beta=beta)
+
+
+def import_blocks(n_rows, n_cols, bf, stage, obs_out, src_out, obs_in, src_in, rows, cols,
+                  identity, data_off, data, obs_csr, src_csr, ctx: Context | None = None):
+    """Upload reference-style factors (``bf_import_factors``) -> ``Operator``."""
+    ctx = ctx or default_context()
+    keep = dict(
+        bf=np.ascontiguousarray(bf, np.int32), stage=np.ascontiguousarray(stage, np.int32),
+        obs_out=np.ascontiguousarray(obs_out, np.int64),
+        src_out=np.ascontiguousarray(src_out, np.int64),
+        obs_in=np.ascontiguousarray(obs_in, np.int64), src_in=np.ascontiguousarray(src_in, np.int64),
+        rows=np.ascontiguousarray(rows, np.int32), cols=np.ascontiguousarray(cols, np.int32),
+        identity=np.ascontiguousarray(identity, np.int8),
+        data_off=np.ascontiguousarray(data_off, np.int64),
+        data=np.ascontiguousarray(data, np.complex128),
+        optr=np.ascontiguousarray(obs_csr[0], np.int64), oidx=np.ascontiguousarray(obs_csr[1], np.int64),
+        sptr=np.ascontiguousarray(src_csr[0], np.int64), sidx=np.ascontiguousarray(src_csr[1], np.int64))
+    d = FactorDesc()
+    d.n_rows, d.n_cols, d.n_blocks = int(n_rows), int(n_cols), len(keep["bf"])
+    d.bf = _p(keep["bf"], C.c_int32)
+    d.stage = _p(keep["stage"], C.c_int32)
+    d.obs_out = _p(keep["obs_out"], C.c_int64)
+    d.src_out = _p(keep["src_out"], C.c_int64)
+    d.obs_in = _p(keep["obs_in"], C.c_int64)
+    d.src_in = _p(keep["src_in"], C.c_int64)
+    d.rows = _p(keep["rows"], C.c_int32)
+    d.cols = _p(keep["cols"], C.c_int32)
+    d.identity = _p(keep["identity"], C.c_int8)
+    d.data_off = _p(keep["data_off"], C.c_int64)
+    d.data = keep["data"].ctypes.data_as(C.POINTER(C.c_double))
+    d.n_obs_nodes = len(keep["optr"]) - 1
+    d.obs_ptr = _p(keep["optr"], C.c_int64)
+    d.obs_idx = _p(keep["oidx"], C.c_int64)
+    d.n_src_nodes = len(keep["sptr"]) - 1
+    d.src_ptr = _p(keep["sptr"], C.c_int64)
+    d.src_idx = _p(keep["sidx"], C.c_int64)
+    h = C.c_void_p()
+    check(load().bf_import_factors(ctx._h, C.byref(d), C.byref(h)), "bf_import_factors")
+    return Operator(h.value, ctx)
+
+
+def _build(obs, src, tree_o: Tree, tree_s: Tree, pairs, k, tol, c_tau, adaptive, seed,
+           min_samples, rank_mode, surrogate, keep_mixed, ctx):
+    lib = load()
+    ctx = ctx or default_context()
+    obs = np.ascontiguousarray(obs, np.float64)
+    src = np.ascontiguousarray(src, np.float64)
+    pairs = np.asarray(pairs, np.int64).reshape(-1, 2)
+    fo = np.ascontiguousarray(pairs[:, 0])
+    fs = np.ascontiguousarray(pairs[:, 1])
+    o = BuildOpts()
+    lib.bf_build_opts_default(C.byref(o))
+    o.c_tau = float(c_tau)
+    o.min_samples = int(min_samples)
+    o.adaptive = int(bool(adaptive))
+    o.seed = int(seed) & ((1 << 64) - 1)
+    o.rank_mode = int(rank_mode)
+    o.keep_mixed = int(bool(keep_mixed))
+    w = None
+    if surrogate is not None:
+        w = np.ascontiguousarray(surrogate, np.float32)
+        o.surrogate_weights = w.ctypes.data_as(C.POINTER(C.c_float))
+        o.surrogate_nweights = w.size
+    h = C.c_void_p()
+    check(lib.bf_build(ctx._h, _p(obs, C.c_double), obs.shape[0], _p(src, C.c_double), src.shape[0],
+                       tree_o._h, tree_s._h, _p(fo, C.c_int64), _p(fs, C.c_int64), len(fo),
+                       float(k), float(tol), C.byref(o), C.byref(h)), "bf_build")
+    return Operator(h.value, ctx)
+
+
+def assemble_BF(obs, src, tree_o: Tree, tree_s: Tree, no: int, ns: int, k: float, tau: float,
+                c_tau: float = 4.0, adaptive: bool = True, seed: int = 0, min_samples: int = 10,
+                rank_mode: int = 0, surrogate=None, keep_mixed: bool = True,
+                ctx: Context | None = None) -> Operator:
+    """``assemble_BF(kernel, blktree, no, ns, k, tau)`` on the GPU (one far block)."""
+    return _build(obs, src, tree_o, tree_s, [(no, ns)], k, tau, c_tau, adaptive, seed,
+                  min_samples, rank_mode, surrogate, keep_mixed, ctx)
+
+
+def PetrovGalerkinBF(obs, src, tree_o: Tree, tree_s: Tree, k: float, tol: float = 1e-3,
+                     alpha: float = 1.0, c_tau: float = 2.9592, adaptive: bool = True,
+                     seed: int = 0, minbflvl: int = 3, leafcomp: bool = True,
+                     min_samples: int = 10, rank_mode: int = 0, surrogate=None,
+                     keep_mixed: bool = True, ctx: Context | None = None) -> Operator:
+    """Far-field part of ``PetrovGalerkinBF`` (``farfieldonly=true``) on the GPU."""
+    far, _ = nearandfar(tree_o, tree_s, alpha, minbflvl, leafcomp)
+    return _build(obs, src, tree_o, tree_s, far, k, tol, c_tau, adaptive, seed, min_samples,
+                  rank_mode, surrogate, keep_mixed, ctx)

@@ -1,0 +1,329 @@
+// C ABI entry points of libbfgpu (declared in include/bfgpu.h).
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "bf_internal.h"
+
+namespace bfg {
+
+static thread_local char g_err[1024] = "";
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+const char* last_error() { return g_err; }
+
+}  // namespace bfg
+
+using namespace bfg;
+
+struct bf_context {
+  Context c;
+};
+struct bf_operator {
+  Operator op;
+};
+
+#define BF_GUARD_BEGIN try {
+#define BF_GUARD_END                                        \
+  }                                                         \
+  catch (const std::bad_alloc&) {                           \
+    set_error("host allocation failed");                    \
+    return BF_ENOMEM;                                       \
+  }                                                         \
+  catch (...) {                                             \
+    set_error("unexpected internal error");                 \
+    return BF_EINVAL;                                       \
+  }
+
+extern "C" {
+
+int bf_version(void) { return 10000; }
+
+const char* bf_status_string(int s) {
+  switch (s) {
+    case BF_OK: return "BF_OK";
+    case BF_EINVAL: return "BF_EINVAL";
+    case BF_ENOMEM: return "BF_ENOMEM";
+    case BF_ECUDA: return "BF_ECUDA";
+    case BF_ETIMEOUT: return "BF_ETIMEOUT";
+    case BF_ENOTSUP: return "BF_ENOTSUP";
+    case BF_ESTATE: return "BF_ESTATE";
+    default: return "BF_UNKNOWN";
+  }
+}
+
+const char* bf_last_error(void) { return last_error(); }
+
+int bf_ctx_create(int device, bf_ctx_t* out) {
+  BF_GUARD_BEGIN
+  if (!out) {
+    set_error("bf_ctx_create: out is NULL");
+    return BF_EINVAL;
+  }
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    set_error("bf_ctx_create: no CUDA device (%s)", cudaGetErrorString(e));
+    return BF_ECUDA;
+  }
+  if (device < 0 || device >= n) {
+    set_error("bf_ctx_create: device %d out of range (%d devices)", device, n);
+    return BF_EINVAL;
+  }
+  auto* h = new bf_context;
+  h->c.device = device;
+  if (cudaGetDeviceProperties(&h->c.prop, device) != cudaSuccess ||
+      cudaSetDevice(device) != cudaSuccess) {
+    cudaGetLastError();
+    delete h;
+    set_error("bf_ctx_create: cannot use device %d", device);
+    return BF_ECUDA;
+  }
+  if (h->c.prop.major < 10) {
+    set_error("bf_ctx_create: device %d is sm_%d%d; this build targets sm_103a", device,
+              h->c.prop.major, h->c.prop.minor);
+    delete h;
+    return BF_ECUDA;
+  }
+  *out = h;
+  return BF_OK;
+  BF_GUARD_END
+}
+
+int bf_ctx_destroy(bf_ctx_t ctx) {
+  delete ctx;
+  return BF_OK;
+}
+
+void bf_build_opts_default(bf_build_opts* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->c_tau = 4.0;
+  o->min_samples = 10;
+  o->adaptive = 1;
+  o->seed = 0;
+  o->rank_mode = 0;
+  o->keep_mixed = 1;
+}
+
+int bf_import_factors(bf_ctx_t ctx, const bf_factor_desc* d, bf_op_t* out) {
+  BF_GUARD_BEGIN
+  if (!ctx || !d || !out) {
+    set_error("bf_import_factors: NULL argument");
+    return BF_EINVAL;
+  }
+  *out = nullptr;
+  if (d->n_blocks <= 0 || !d->bf || !d->stage || !d->obs_out || !d->src_out || !d->obs_in ||
+      !d->src_in || !d->rows || !d->cols || !d->identity || !d->data_off || !d->obs_ptr ||
+      !d->obs_idx || !d->src_ptr || !d->src_idx || d->n_rows <= 0 || d->n_cols <= 0) {
+    set_error("bf_import_factors: incomplete descriptor");
+    return BF_EINVAL;
+  }
+  auto* h = new bf_operator;
+  Operator& op = h->op;
+  op.ctx = &ctx->c;
+  Logical& lg = op.logical;
+  lg.n_rows = d->n_rows;
+  lg.n_cols = d->n_cols;
+  auto load_vm = [&](ValuesMap& vm, int64_t nn, const int64_t* ptr, const int64_t* idx,
+                     int64_t npts) -> bool {
+    vm.ptr.assign(ptr, ptr + nn + 1);
+    if (vm.ptr[0] != 0) return false;
+    for (int64_t i = 0; i < nn; ++i)
+      if (vm.ptr[i + 1] < vm.ptr[i]) return false;
+    vm.idx.assign(idx, idx + vm.ptr[nn]);
+    for (int64_t v : vm.idx)
+      if (v < 0 || v >= npts) return false;
+    return true;
+  };
+  if (!load_vm(lg.obs_vals, d->n_obs_nodes, d->obs_ptr, d->obs_idx, d->n_rows) ||
+      !load_vm(lg.src_vals, d->n_src_nodes, d->src_ptr, d->src_idx, d->n_cols)) {
+    delete h;
+    set_error("bf_import_factors: malformed node->values map");
+    return BF_EINVAL;
+  }
+  int64_t raw_n = 0;
+  int32_t nbf = 0;
+  lg.blocks.resize(d->n_blocks);
+  for (int64_t b = 0; b < d->n_blocks; ++b) {
+    LBlock& k = lg.blocks[b];
+    k.bf = d->bf[b];
+    k.stage = d->stage[b];
+    k.oo = d->obs_out[b];
+    k.so = d->src_out[b];
+    k.oi = d->obs_in[b];
+    k.si = d->src_in[b];
+    k.ident = d->identity[b] ? 1 : 0;
+    k.rows = k.ident ? 0 : d->rows[b];
+    k.cols = k.ident ? 0 : d->cols[b];
+    k.raw_off = d->data_off[b];
+    k.raw_ld = std::max(k.rows, 1);
+    if (!k.ident) {
+      if (k.rows < 0 || k.cols < 0 || k.raw_off < 0) {
+        delete h;
+        set_error("bf_import_factors: block %lld has invalid size/offset", (long long)b);
+        return BF_EINVAL;
+      }
+      raw_n = std::max(raw_n, k.raw_off + (int64_t)k.rows * k.cols);
+    }
+    nbf = std::max(nbf, k.bf + 1);
+  }
+  lg.n_bf = nbf;
+  if (raw_n > 0 && !d->data) {
+    delete h;
+    set_error("bf_import_factors: data is NULL");
+    return BF_EINVAL;
+  }
+  int s = pack_plan(lg, op.plan);
+  if (s != BF_OK) {
+    delete h;
+    return s;
+  }
+  if (cudaSetDevice(ctx->c.device) != cudaSuccess) {
+    cudaGetLastError();
+    delete h;
+    set_error("bf_import_factors: cudaSetDevice failed");
+    return BF_ECUDA;
+  }
+  op.raw_is_double = 1;
+  op.raw_entries = raw_n;
+  if (cudaMalloc(&op.d_raw, (size_t)std::max<int64_t>(raw_n, 1) * 2 * sizeof(double)) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    delete h;
+    set_error("bf_import_factors: cannot allocate raw factor storage");
+    return BF_ENOMEM;
+  }
+  if (raw_n > 0 && cudaMemcpy(op.d_raw, d->data, (size_t)raw_n * 2 * sizeof(double),
+                              cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaGetLastError();
+    delete h;
+    set_error("bf_import_factors: upload failed");
+    return BF_ECUDA;
+  }
+  s = upload_plan(op);
+  if (s != BF_OK) {
+    delete h;
+    return s;
+  }
+  *out = h;
+  return BF_OK;
+  BF_GUARD_END
+}
+
+int bf_matvec(bf_op_t op, int trans, int64_t nrhs, const double* x, int64_t ldx, double* y,
+              int64_t ldy, const double* alpha, const double* beta, int ptr_mode, void* stream) {
+  BF_GUARD_BEGIN
+  if (!op) {
+    set_error("bf_matvec: NULL operator");
+    return BF_EINVAL;
+  }
+  return run_matvec(op->op, trans, nrhs, x, ldx, y, ldy, alpha, beta, ptr_mode,
+                    (cudaStream_t)stream);
+  BF_GUARD_END
+}
+
+int bf_op_size(bf_op_t op, int64_t* n_rows, int64_t* n_cols) {
+  if (!op) {
+    set_error("bf_op_size: NULL operator");
+    return BF_EINVAL;
+  }
+  if (n_rows) *n_rows = op->op.plan.n_rows;
+  if (n_cols) *n_cols = op->op.plan.n_cols;
+  return BF_OK;
+}
+
+int bf_op_stats_get(bf_op_t op, bf_op_stats* st) {
+  if (!op || !st) {
+    set_error("bf_op_stats_get: NULL argument");
+    return BF_EINVAL;
+  }
+  *st = op->op.stats;
+  return BF_OK;
+}
+
+int bf_op_export_blocks(bf_op_t h, int64_t* n_blocks, int64_t* n_data, int32_t* bf,
+                        int32_t* stage, int64_t* obs_out, int64_t* src_out, int64_t* obs_in,
+                        int64_t* src_in, int32_t* rows, int32_t* cols, int8_t* identity,
+                        int64_t* data_off, double* data) {
+  BF_GUARD_BEGIN
+  if (!h || !n_blocks || !n_data) {
+    set_error("bf_op_export_blocks: NULL argument");
+    return BF_EINVAL;
+  }
+  Operator& op = h->op;
+  const auto& B = op.logical.blocks;
+  int64_t tot = 0;
+  for (const auto& k : B)
+    if (!k.ident) tot += (int64_t)k.rows * k.cols;
+  *n_blocks = (int64_t)B.size();
+  *n_data = tot;
+  if (!data) return BF_OK;
+  if (!bf || !stage || !obs_out || !src_out || !obs_in || !src_in || !rows || !cols ||
+      !identity || !data_off) {
+    set_error("bf_op_export_blocks: NULL output array");
+    return BF_EINVAL;
+  }
+  if (!op.d_raw) {
+    set_error("bf_op_export_blocks: raw factors were released");
+    return BF_ESTATE;
+  }
+  BF_TRY_CUDA(cudaSetDevice(op.ctx->device));
+  size_t esz = op.raw_is_double ? 16 : 8;
+  std::vector<char> raw((size_t)op.raw_entries * esz);
+  BF_TRY_CUDA(cudaMemcpy(raw.data(), op.d_raw, raw.size(), cudaMemcpyDeviceToHost));
+  int64_t off = 0;
+  for (size_t b = 0; b < B.size(); ++b) {
+    const LBlock& k = B[b];
+    bf[b] = k.bf;
+    stage[b] = k.stage;
+    obs_out[b] = k.oo;
+    src_out[b] = k.so;
+    obs_in[b] = k.oi;
+    src_in[b] = k.si;
+    rows[b] = k.rows;
+    cols[b] = k.cols;
+    identity[b] = k.ident;
+    data_off[b] = off;
+    if (k.ident) continue;
+    for (int32_t j = 0; j < k.cols; ++j)
+      for (int32_t i = 0; i < k.rows; ++i) {
+        size_t src = (size_t)(k.raw_off + (int64_t)j * k.raw_ld + i);
+        double re, im;
+        if (op.raw_is_double) {
+          const double* p = (const double*)raw.data() + 2 * src;
+          re = p[0];
+          im = p[1];
+        } else {
+          const float* p = (const float*)raw.data() + 2 * src;
+          re = p[0];
+          im = p[1];
+        }
+        data[2 * (off + (int64_t)j * k.rows + i)] = re;
+        data[2 * (off + (int64_t)j * k.rows + i) + 1] = im;
+      }
+    off += (int64_t)k.rows * k.cols;
+  }
+  return BF_OK;
+  BF_GUARD_END
+}
+
+int bf_op_destroy(bf_op_t op) {
+  if (op) {
+    cudaSetDevice(op->op.ctx->device);
+    delete op;
+  }
+  return BF_OK;
+}
+
+}  // extern "C"

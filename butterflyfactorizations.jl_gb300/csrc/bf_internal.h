@@ -1,0 +1,157 @@
+// Internal declarations of libbfgpu (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "bfgpu.h"
+
+namespace bfg {
+
+// ---------------------------------------------------------------- errors
+void set_error(const char* fmt, ...);
+const char* last_error();
+
+#define BF_TRY_CUDA(call)                                                              \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess) {                                                           \
+      bfg::set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                     __LINE__);                                                        \
+      return BF_ECUDA;                                                                 \
+    }                                                                                  \
+  } while (0)
+
+#define BF_TRY(call)              \
+  do {                            \
+    int s_ = (call);              \
+    if (s_ != BF_OK) return s_;   \
+  } while (0)
+
+// ---------------------------------------------------------------- trees
+struct Tree {
+  int64_t n_points = 0;
+  std::vector<double> center;  // 3 * n_nodes
+  std::vector<double> half;
+  std::vector<int32_t> level, parent, first_child, n_child;
+  std::vector<int64_t> begin, end, perm;
+  int64_t nn() const { return (int64_t)half.size(); }
+  bool isleaf(int64_t n) const { return n_child[n] == 0; }
+  int64_t nvals(int64_t n) const { return end[n] - begin[n]; }
+  const int64_t* vals(int64_t n) const { return perm.data() + begin[n]; }
+  double radius(int64_t n) const;
+  int32_t depth() const;
+};
+
+int tree_build(const double* xyz, int64_t n, int32_t max_points, int32_t max_depth, Tree& t);
+// BFS levels below root with shallow leaves pushed down (src/auxillaries.jl:263-350).
+std::vector<std::vector<int64_t>> traverse_and_pad(const Tree& t, int64_t root);
+bool is_far(const Tree& ts, const Tree& to, int64_t snode, int64_t onode, double alpha);
+
+// ---------------------------------------------------------------- logical factors
+// One reference ButterflyBlock (bfstructs.jl:21-29) whose matrix lives in a raw
+// device array (column-major, leading dimension raw_ld).
+struct LBlock {
+  int32_t bf;
+  int32_t stage;  // 0 = Q, l = R level l, -1 = P
+  int64_t oo, so, oi, si;
+  int32_t rows, cols;
+  int8_t ident;
+  int64_t raw_off;
+  int32_t raw_ld;
+};
+
+// node -> values map (CSR), 0-based point indices
+struct ValuesMap {
+  std::vector<int64_t> ptr, idx;
+  int64_t n(int64_t node) const { return ptr[node + 1] - ptr[node]; }
+  const int64_t* v(int64_t node) const { return idx.data() + ptr[node]; }
+};
+
+struct Logical {
+  int64_t n_rows = 0, n_cols = 0;
+  int32_t n_bf = 0;
+  std::vector<LBlock> blocks;
+  ValuesMap obs_vals, src_vals;
+};
+
+// ---------------------------------------------------------------- packed plan
+enum : int32_t { TASK_DENSE = 0, TASK_COPY = 1 };
+
+// Device task descriptor: row side = rmap[0..M), column side = cmap[0..n);
+// forward computes ws[rmap] = A * ws[cmap]; adjoint ws[cmap] = A^H * ws[rmap].
+struct alignas(16) DTask {
+  long long a_off;     // first complex entry of the M x n column-major matrix
+  long long rmap_off;  // offset into the routing array
+  long long cmap_off;
+  int M, n, kind, pad;
+};
+static_assert(sizeof(DTask) == 48, "DTask layout");
+
+// Copy of one logical block into a task matrix (repack on the device).
+struct alignas(16) DSeg {
+  long long src_off;  // raw array offset (complex entries)
+  long long dst_off;  // packed matrix offset of the block's (0,0) entry
+  int src_ld, dst_ld, rows, cols;
+  int kind;  // 0 = copy, 1 = identity
+  int pad[3];
+};
+static_assert(sizeof(DSeg) == 48, "DSeg layout");
+
+struct Plan {
+  int64_t n_rows = 0, n_cols = 0;
+  int64_t xg_off = 0, yg_off = 0;  // x-space and y-space regions of the workspace
+  int64_t ws_entries = 0;
+  std::vector<DTask> tasks;
+  std::vector<int64_t> stage_begin;  // n_stages + 1
+  std::vector<int32_t> maps;
+  int64_t a_entries = 0;
+  std::vector<DSeg> segs;
+  bool yg_covered = false, xg_covered = false;
+  int64_t alg_bytes_fwd = 0;
+  int64_t block_entries = 0;
+  int64_t max_rank = 0;
+  int32_t n_bf = 0;
+  int64_t n_stages() const { return (int64_t)stage_begin.size() - 1; }
+};
+
+int pack_plan(const Logical& lg, Plan& plan);
+
+// ---------------------------------------------------------------- device-side
+struct Context {
+  int device = 0;
+  cudaDeviceProp prop{};
+};
+
+struct Operator {
+  Context* ctx = nullptr;
+  cudaStream_t stream = nullptr;
+  Plan plan;
+  Logical logical;
+  int raw_is_double = 1;
+  void* d_raw = nullptr;  // raw logical block data (double2 or float2)
+  int64_t raw_entries = 0;
+  // plain (FP64-accurate) operator: float-float factors
+  float4* d_A = nullptr;
+  DTask* d_tasks = nullptr;
+  int32_t* d_maps = nullptr;
+  float4* d_ws = nullptr;
+  // staging of host right-hand sides
+  double* d_x = nullptr;
+  double* d_y = nullptr;
+  int64_t stage_cap = 0;
+  // mixed path
+  void* mixed = nullptr;
+  bf_op_stats stats{};
+  ~Operator();
+};
+
+int upload_plan(Operator& op);  // repacks d_raw into d_A, uploads tasks/maps, allocates ws
+int run_matvec(Operator& op, int trans, int64_t nrhs, const double* x, int64_t ldx, double* y,
+               int64_t ldy, const double* alpha, const double* beta, int ptr_mode,
+               cudaStream_t stream);
+
+}  // namespace bfg

@@ -1,0 +1,379 @@
+// FP64-accurate butterfly matvec on the GPU (one right-hand side per pass).
+//
+// The level sequence of the reference flat matvec (src/Butterflyalgebra/
+// bfvector.jl:200-296: Q gather+GEMV, R levels, P GEMV+scatter-add) over all
+// far blocks of an operator becomes one launch per level.  Each launch runs
+// independent dense tasks (see bf_pack.cpp); a task reads its input vector
+// through a routing map (the fused inter-level gather) and writes each output
+// entry exactly once (no atomics, deterministic).  The adjoint and transpose
+// walk the same tasks backwards with A^H / A^T, reusing the forward factors.
+//
+// Arithmetic: factors and vectors are float-float pairs (bf_dfloat.cuh), so
+// products run on the FP32 pipes at ~1e-14 relative accuracy; GB300's FP64
+// rate (about 1.2 TFLOP/s) cannot feed 8 flop per 16 B at HBM speed.
+#include <algorithm>
+
+#include "bf_dfloat.cuh"
+#include "bf_internal.h"
+
+namespace bfg {
+namespace {
+
+constexpr int NT = 256;   // threads per task CTA
+constexpr int CH = 2048;  // staged matrix entries per chunk (32 KB)
+constexpr int XC = 512;   // staged input entries per chunk
+constexpr int RPT = 4;    // rows per thread per row tile (forward)
+
+__device__ __forceinline__ int pow2_threads(int m) {
+  return m <= 32 ? 32 : (m <= 64 ? 64 : (m <= 128 ? 128 : 256));
+}
+
+// forward: ws[rmap[i]] = sum_j A[i,j] ws[cmap[j]]
+__global__ void __launch_bounds__(NT) stage_fwd_kernel(const DTask* __restrict__ tasks,
+                                                       const float4* __restrict__ A,
+                                                       const int32_t* __restrict__ maps,
+                                                       float4* __restrict__ ws) {
+  __shared__ float4 sA[CH];
+  __shared__ float4 sx[XC];
+  const DTask t = tasks[blockIdx.x];
+  const int32_t* __restrict__ rmap = maps + t.rmap_off;
+  const int32_t* __restrict__ cmap = maps + t.cmap_off;
+  const int tid = threadIdx.x;
+  if (t.kind == TASK_COPY) {
+    for (int i = tid; i < t.M; i += NT) ws[rmap[i]] = ws[cmap[i]];
+    return;
+  }
+  const int M = t.M, n = t.n;
+  const float4* __restrict__ Ag = A + t.a_off;
+  const int P = pow2_threads(M);
+  const int S = NT / P;
+  const int p = tid % P, s = tid / P;
+  for (int r0 = 0; r0 < M; r0 += P * RPT) {
+    const int TR = min(M - r0, P * RPT);
+    int TC = max(1, CH / TR);
+    TC = min(TC, XC);
+    float4 acc[RPT];
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int c0 = 0; c0 < n; c0 += TC) {
+      const int tc = min(TC, n - c0);
+      const float4* __restrict__ src = Ag + (size_t)c0 * M + r0;
+      if (TR == M) {
+        const int tot = tc * TR;  // contiguous columns
+        for (int e = tid; e < tot; e += NT) sA[e] = __ldg(src + e);
+      } else {
+        for (int e = tid; e < tc * TR; e += NT) {
+          int jj = e / TR, ii = e - jj * TR;
+          sA[e] = __ldg(src + (size_t)jj * M + ii);
+        }
+      }
+      for (int e = tid; e < tc; e += NT) sx[e] = ws[cmap[c0 + e]];
+      __syncthreads();
+      for (int jj = s; jj < tc; jj += S) {
+        const float4 xv = sx[jj];
+#pragma unroll
+        for (int k = 0; k < RPT; ++k) {
+          int ii = p + k * P;
+          if (ii < TR) cdf_mac(acc[k], sA[jj * TR + ii], xv);
+        }
+      }
+      __syncthreads();
+    }
+    // reduce the S column splits and write
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+      int ii = p + k * P;
+      if (S > 1) {
+        sA[tid] = acc[k];
+        __syncthreads();
+        if (s == 0 && ii < TR) {
+          float4 v = sA[p];
+          for (int q = 1; q < S; ++q) cdf_add(v, sA[p + q * P]);
+          ws[rmap[r0 + ii]] = cdf_norm(v);
+        }
+        __syncthreads();
+      } else if (ii < TR) {
+        ws[rmap[r0 + ii]] = cdf_norm(acc[k]);
+      }
+    }
+  }
+}
+
+// adjoint (CONJ) or transpose: ws[cmap[j]] = sum_i op(A[i,j]) ws[rmap[i]]
+template <bool CONJ>
+__global__ void __launch_bounds__(NT) stage_adj_kernel(const DTask* __restrict__ tasks,
+                                                       const float4* __restrict__ A,
+                                                       const int32_t* __restrict__ maps,
+                                                       float4* __restrict__ ws) {
+  __shared__ float4 sA[CH + NT];
+  __shared__ float4 sv[CH / 32];
+  const DTask t = tasks[blockIdx.x];
+  const int32_t* __restrict__ rmap = maps + t.rmap_off;
+  const int32_t* __restrict__ cmap = maps + t.cmap_off;
+  const int tid = threadIdx.x;
+  if (t.kind == TASK_COPY) {
+    for (int i = tid; i < t.M; i += NT) ws[cmap[i]] = ws[rmap[i]];
+    return;
+  }
+  const int M = t.M, n = t.n;
+  const float4* __restrict__ Ag = A + t.a_off;
+  const int Pc = pow2_threads(n);
+  const int S = NT / Pc;
+  const int q = tid % Pc, s = tid / Pc;
+  const int TRmax = CH / Pc;  // >= 8, power of two
+  const int LDS = TRmax + 1;  // odd stride: conflict-free column reads
+  for (int c0 = 0; c0 < n; c0 += Pc) {
+    const int tc = min(Pc, n - c0);
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int r0 = 0; r0 < M; r0 += TRmax) {
+      const int tr = min(TRmax, M - r0);
+      const float4* __restrict__ src = Ag + (size_t)c0 * M + r0;
+      for (int e = tid; e < tc * tr; e += NT) {
+        int jj = e / tr, ii = e - jj * tr;
+        sA[jj * LDS + ii] = __ldg(src + (size_t)jj * M + ii);
+      }
+      for (int e = tid; e < tr; e += NT) sv[e] = ws[rmap[r0 + e]];
+      __syncthreads();
+      if (q < tc) {
+        for (int ii = s; ii < tr; ii += S) {
+          const float4 a = sA[q * LDS + ii];
+          if (CONJ)
+            cdf_mac_conj(acc, a, sv[ii]);
+          else
+            cdf_mac(acc, a, sv[ii]);
+        }
+      }
+      __syncthreads();
+    }
+    if (S > 1) {
+      sA[tid] = acc;
+      __syncthreads();
+      if (s == 0 && q < tc) {
+        float4 v = sA[q];
+        for (int r = 1; r < S; ++r) cdf_add(v, sA[q + r * Pc]);
+        ws[cmap[c0 + q]] = cdf_norm(v);
+      }
+      __syncthreads();
+    } else if (q < tc) {
+      ws[cmap[c0 + q]] = cdf_norm(acc);
+    }
+  }
+}
+
+// raw logical blocks -> packed float-float task matrices
+template <typename SrcT>
+__global__ void repack_kernel(const DSeg* __restrict__ segs, const SrcT* __restrict__ raw,
+                              float4* __restrict__ A) {
+  const DSeg g = segs[blockIdx.x];
+  if (g.kind == 1) {
+    for (int i = threadIdx.x; i < g.rows; i += blockDim.x)
+      A[g.dst_off + (size_t)i * g.dst_ld + i] = make_float4(1.f, 0.f, 0.f, 0.f);
+    return;
+  }
+  const long long tot = (long long)g.rows * g.cols;
+  for (long long e = threadIdx.x; e < tot; e += blockDim.x) {
+    int j = (int)(e / g.rows), i = (int)(e - (long long)j * g.rows);
+    SrcT v = raw[g.src_off + (size_t)j * g.src_ld + i];
+    float4 o;
+    if constexpr (sizeof(SrcT) == 16) {
+      float2 re = df_split(v.x), im = df_split(v.y);
+      o = make_float4(re.x, re.y, im.x, im.y);
+    } else {
+      o = make_float4(v.x, 0.f, v.y, 0.f);
+    }
+    A[g.dst_off + (size_t)j * g.dst_ld + i] = o;
+  }
+}
+
+// x (complex double, n entries) -> ws[off + i] (complex float-float); optional conj
+__global__ void split_kernel(const double2* __restrict__ x, int64_t n, float4* __restrict__ ws,
+                             int64_t off, int conj) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double2 v = x[i];
+    float2 re = df_split(v.x), im = df_split(conj ? -v.y : v.y);
+    ws[off + i] = make_float4(re.x, re.y, im.x, im.y);
+  }
+}
+
+// y = beta*y + alpha*v, v = ws[off + i] (optionally conjugated first)
+__global__ void combine_kernel(double2* __restrict__ y, int64_t n, const float4* __restrict__ ws,
+                               int64_t off, double2 alpha, double2 beta, int beta_zero,
+                               int conj) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float4 a = ws[off + i];
+    double vr = (double)a.x + (double)a.y;
+    double vi = (double)a.z + (double)a.w;
+    if (conj) vi = -vi;
+    double2 o;
+    o.x = alpha.x * vr - alpha.y * vi;
+    o.y = alpha.x * vi + alpha.y * vr;
+    if (!beta_zero) {
+      double2 yo = y[i];
+      o.x += beta.x * yo.x - beta.y * yo.y;
+      o.y += beta.x * yo.y + beta.y * yo.x;
+    }
+    y[i] = o;
+  }
+}
+
+inline int grid_for(int64_t n, int threads) {
+  int64_t g = (n + threads - 1) / threads;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 16));
+}
+
+}  // namespace
+
+Operator::~Operator() {
+  if (d_raw) cudaFree(d_raw);
+  if (d_A) cudaFree(d_A);
+  if (d_tasks) cudaFree(d_tasks);
+  if (d_maps) cudaFree(d_maps);
+  if (d_ws) cudaFree(d_ws);
+  if (d_x) cudaFree(d_x);
+  if (d_y) cudaFree(d_y);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+int upload_plan(Operator& op) {
+  Plan& p = op.plan;
+  BF_TRY_CUDA(cudaSetDevice(op.ctx->device));
+  if (!op.stream) BF_TRY_CUDA(cudaStreamCreateWithFlags(&op.stream, cudaStreamNonBlocking));
+  size_t abytes = (size_t)std::max<int64_t>(p.a_entries, 1) * sizeof(float4);
+  if (cudaMalloc(&op.d_A, abytes) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("upload: cannot allocate %zu bytes of factors", abytes);
+    return BF_ENOMEM;
+  }
+  BF_TRY_CUDA(cudaMemsetAsync(op.d_A, 0, abytes, op.stream));
+  if (!p.segs.empty()) {
+    DSeg* d_segs = nullptr;
+    BF_TRY_CUDA(cudaMalloc(&d_segs, p.segs.size() * sizeof(DSeg)));
+    BF_TRY_CUDA(cudaMemcpyAsync(d_segs, p.segs.data(), p.segs.size() * sizeof(DSeg),
+                                cudaMemcpyHostToDevice, op.stream));
+    // gridDim.x limit is 2^31-1; segment counts stay far below
+    if (op.raw_is_double)
+      repack_kernel<double2><<<(unsigned)p.segs.size(), 128, 0, op.stream>>>(
+          d_segs, (const double2*)op.d_raw, op.d_A);
+    else
+      repack_kernel<float2><<<(unsigned)p.segs.size(), 128, 0, op.stream>>>(
+          d_segs, (const float2*)op.d_raw, op.d_A);
+    BF_TRY_CUDA(cudaGetLastError());
+    BF_TRY_CUDA(cudaStreamSynchronize(op.stream));
+    cudaFree(d_segs);
+  }
+  BF_TRY_CUDA(cudaMalloc(&op.d_tasks, std::max<size_t>(1, p.tasks.size()) * sizeof(DTask)));
+  BF_TRY_CUDA(cudaMemcpy(op.d_tasks, p.tasks.data(), p.tasks.size() * sizeof(DTask),
+                         cudaMemcpyHostToDevice));
+  BF_TRY_CUDA(cudaMalloc(&op.d_maps, std::max<size_t>(1, p.maps.size()) * sizeof(int32_t)));
+  BF_TRY_CUDA(cudaMemcpy(op.d_maps, p.maps.data(), p.maps.size() * sizeof(int32_t),
+                         cudaMemcpyHostToDevice));
+  if (cudaMalloc(&op.d_ws, (size_t)std::max<int64_t>(p.ws_entries, 1) * sizeof(float4)) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    set_error("upload: cannot allocate workspace");
+    return BF_ENOMEM;
+  }
+  BF_TRY_CUDA(cudaMemset(op.d_ws, 0, (size_t)std::max<int64_t>(p.ws_entries, 1) * sizeof(float4)));
+  op.stats.n_bf = p.n_bf;
+  op.stats.n_stages = p.n_stages();
+  op.stats.n_tasks = (int64_t)p.tasks.size();
+  op.stats.factor_entries = p.a_entries;
+  op.stats.factor_bytes = p.a_entries * (int64_t)sizeof(float4);
+  op.stats.workspace_entries = p.ws_entries;
+  op.stats.map_entries = (int64_t)p.maps.size();
+  op.stats.alg_bytes_fwd = p.alg_bytes_fwd;
+  op.stats.max_rank = p.max_rank;
+  return BF_OK;
+}
+
+// One FP64-accurate matvec of a single right-hand side, device pointers.
+static int matvec_one(Operator& op, int trans, const double2* x, double2* y, double2 alpha,
+                      double2 beta, cudaStream_t st) {
+  const Plan& p = op.plan;
+  const bool fwd = trans == BF_OP_N;
+  const int64_t nin = fwd ? p.n_cols : p.n_rows;
+  const int64_t nout = fwd ? p.n_rows : p.n_cols;
+  const int64_t in_off = fwd ? p.xg_off : p.yg_off;
+  const int64_t out_off = fwd ? p.yg_off : p.xg_off;
+  const bool covered = fwd ? p.yg_covered : p.xg_covered;
+  split_kernel<<<grid_for(nin, 256), 256, 0, st>>>(x, nin, op.d_ws, in_off, 0);
+  if (!covered)
+    BF_TRY_CUDA(cudaMemsetAsync(op.d_ws + out_off, 0, (size_t)nout * sizeof(float4), st));
+  const int64_t ns = p.n_stages();
+  for (int64_t k = 0; k < ns; ++k) {
+    int64_t s = fwd ? k : ns - 1 - k;
+    int64_t b = p.stage_begin[s], e = p.stage_begin[s + 1];
+    if (e <= b) continue;
+    const DTask* tk = op.d_tasks + b;
+    if (fwd)
+      stage_fwd_kernel<<<(unsigned)(e - b), NT, 0, st>>>(tk, op.d_A, op.d_maps, op.d_ws);
+    else if (trans == BF_OP_C)
+      stage_adj_kernel<true><<<(unsigned)(e - b), NT, 0, st>>>(tk, op.d_A, op.d_maps, op.d_ws);
+    else
+      stage_adj_kernel<false><<<(unsigned)(e - b), NT, 0, st>>>(tk, op.d_A, op.d_maps, op.d_ws);
+  }
+  combine_kernel<<<grid_for(nout, 256), 256, 0, st>>>(y, nout, op.d_ws, out_off, alpha, beta,
+                                                      beta.x == 0.0 && beta.y == 0.0, 0);
+  BF_TRY_CUDA(cudaGetLastError());
+  return BF_OK;
+}
+
+int run_matvec(Operator& op, int trans, int64_t nrhs, const double* x, int64_t ldx, double* y,
+               int64_t ldy, const double* alpha, const double* beta, int ptr_mode,
+               cudaStream_t stream) {
+  const Plan& p = op.plan;
+  if (trans != BF_OP_N && trans != BF_OP_C && trans != BF_OP_T) {
+    set_error("bf_matvec: invalid trans %d", trans);
+    return BF_EINVAL;
+  }
+  const int64_t nin = trans == BF_OP_N ? p.n_cols : p.n_rows;
+  const int64_t nout = trans == BF_OP_N ? p.n_rows : p.n_cols;
+  if (nrhs < 0 || (nrhs > 0 && (!x || !y || ldx < nin || ldy < nout))) {
+    set_error("bf_matvec: invalid sizes (nrhs=%lld ldx=%lld ldy=%lld, need %lld/%lld)",
+              (long long)nrhs, (long long)ldx, (long long)ldy, (long long)nin, (long long)nout);
+    return BF_EINVAL;
+  }
+  if (nrhs == 0) return BF_OK;
+  double2 a = make_double2(alpha ? alpha[0] : 1.0, alpha ? alpha[1] : 0.0);
+  double2 b = make_double2(beta ? beta[0] : 0.0, beta ? beta[1] : 0.0);
+  const bool bzero = b.x == 0.0 && b.y == 0.0;
+  BF_TRY_CUDA(cudaSetDevice(op.ctx->device));
+  cudaStream_t st = stream ? stream : op.stream;
+  if (ptr_mode == BF_PTR_DEVICE) {
+    for (int64_t c = 0; c < nrhs; ++c)
+      BF_TRY(matvec_one(op, trans, (const double2*)(x + 2 * c * ldx), (double2*)(y + 2 * c * ldy),
+                        a, b, st));
+    return BF_OK;
+  }
+  if (ptr_mode != BF_PTR_HOST) {
+    set_error("bf_matvec: invalid ptr_mode %d", ptr_mode);
+    return BF_EINVAL;
+  }
+  // host pointers: stage through device buffers (sized to the largest call so far)
+  int64_t need = std::max(p.n_rows, p.n_cols) * nrhs;
+  if (need > op.stage_cap) {
+    if (op.d_x) cudaFree(op.d_x);
+    if (op.d_y) cudaFree(op.d_y);
+    op.d_x = op.d_y = nullptr;
+    op.stage_cap = 0;
+    BF_TRY_CUDA(cudaMalloc(&op.d_x, (size_t)need * 2 * sizeof(double)));
+    BF_TRY_CUDA(cudaMalloc(&op.d_y, (size_t)need * 2 * sizeof(double)));
+    op.stage_cap = need;
+  }
+  BF_TRY_CUDA(cudaMemcpy2DAsync(op.d_x, nin * 2 * sizeof(double), x, ldx * 2 * sizeof(double),
+                                nin * 2 * sizeof(double), nrhs, cudaMemcpyHostToDevice, st));
+  if (!bzero)
+    BF_TRY_CUDA(cudaMemcpy2DAsync(op.d_y, nout * 2 * sizeof(double), y, ldy * 2 * sizeof(double),
+                                  nout * 2 * sizeof(double), nrhs, cudaMemcpyHostToDevice, st));
+  for (int64_t c = 0; c < nrhs; ++c)
+    BF_TRY(matvec_one(op, trans, (const double2*)(op.d_x + 2 * c * nin),
+                      (double2*)(op.d_y + 2 * c * nout), a, b, st));
+  BF_TRY_CUDA(cudaMemcpy2DAsync(y, ldy * 2 * sizeof(double), op.d_y, nout * 2 * sizeof(double),
+                                nout * 2 * sizeof(double), nrhs, cudaMemcpyDeviceToHost, st));
+  BF_TRY_CUDA(cudaStreamSynchronize(st));
+  return BF_OK;
+}
+
+}  // namespace bfg

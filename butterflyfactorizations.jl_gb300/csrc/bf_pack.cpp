@@ -1,0 +1,414 @@
+// Packing of a set of butterfly factorisations into the flat device layout.
+//
+// Input: reference-style blocks (src/ButterflyFactorization/bfstructs.jl:21-29)
+// of many far pairs.  The flat pointers of the reference (one Dict per level,
+// bfstructs.jl:107-143) become "slots": contiguous segments of one workspace
+// array.  Each level becomes one launch of independent tasks:
+//   Q stage : one task per source leaf; the Q blocks of all far pairs on that
+//             leaf stacked vertically, input gathered from x by values(leaf).
+//   R level : one task per connected block set (node pair); its in-slots are
+//             the columns, its out-slots the rows (the column split of one
+//             compressed T in assemble_BF, bfassembly.jl:296-307).
+//   P stage : one task per observer leaf; the P blocks of all far pairs on that
+//             leaf concatenated horizontally, output scattered to y by
+//             values(leaf).
+// Every workspace entry then has exactly one writer per direction, so neither
+// the forward nor the adjoint needs atomics, and the adjoint is the same task
+// list read backwards with rows and columns swapped.
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <unordered_map>
+
+#include "bf_internal.h"
+
+namespace bfg {
+namespace {
+
+struct SlotKey {
+  int32_t bf, level;
+  int64_t o, s;
+  bool operator==(const SlotKey& k) const {
+    return bf == k.bf && level == k.level && o == k.o && s == k.s;
+  }
+};
+struct SlotKeyHash {
+  size_t operator()(const SlotKey& k) const {
+    uint64_t h = 0x9E3779B97F4A7C15ull * (uint64_t)(uint32_t)k.bf;
+    h ^= (uint64_t)k.level + 0x7F4A7C159E3779B9ull + (h << 6) + (h >> 2);
+    h ^= (uint64_t)k.o * 0xBF58476D1CE4E5B9ull + (h << 6) + (h >> 2);
+    h ^= (uint64_t)k.s * 0x94D049BB133111EBull + (h << 6) + (h >> 2);
+    return (size_t)h;
+  }
+};
+
+enum : int8_t { SIDE_SLOT = 0, SIDE_X = 1, SIDE_Y = 2 };
+struct Side {
+  int8_t type;
+  int64_t id;  // slot id or tree node id
+  int64_t len;
+};
+struct Member {
+  int64_t blk;  // logical block (-1 = explicit identity)
+  int32_t row_off, col_off;
+  int32_t ident_n;
+};
+struct TaskB {
+  int32_t stage;
+  int32_t kind;
+  std::vector<Side> rows, cols;
+  std::vector<Member> mats;
+  int64_t M = 0, n = 0;
+};
+
+struct DSU {
+  std::vector<int64_t> p;
+  int64_t find(int64_t x) {
+    while (p[x] != x) x = p[x] = p[p[x]];
+    return x;
+  }
+  void unite(int64_t a, int64_t b) {
+    a = find(a);
+    b = find(b);
+    if (a != b) p[b] = a;
+  }
+};
+
+}  // namespace
+
+int pack_plan(const Logical& lg, Plan& plan) {
+  plan = Plan();
+  plan.n_rows = lg.n_rows;
+  plan.n_cols = lg.n_cols;
+  const auto& B = lg.blocks;
+  int64_t nb = (int64_t)B.size();
+  int32_t n_bf = lg.n_bf;
+  plan.n_bf = n_bf;
+  if (nb == 0 || n_bf <= 0) {
+    set_error("pack: no blocks");
+    return BF_EINVAL;
+  }
+  // ---- per-BF depth (number of levels = #R + 1)
+  std::vector<int32_t> nlev(n_bf, 1);
+  for (int64_t b = 0; b < nb; ++b) {
+    const LBlock& k = B[b];
+    if (k.bf < 0 || k.bf >= n_bf) {
+      set_error("pack: block %lld has bf id %d out of range", (long long)b, k.bf);
+      return BF_EINVAL;
+    }
+    if (k.stage > 0) nlev[k.bf] = std::max(nlev[k.bf], k.stage + 1);
+    if (!k.ident && (k.rows < 0 || k.cols < 0)) {
+      set_error("pack: block %lld has negative size", (long long)b);
+      return BF_EINVAL;
+    }
+  }
+  int32_t Lmax = *std::max_element(nlev.begin(), nlev.end());
+  // block order by (stage rank, original order): Q, R1, R2, ..., P
+  auto srank = [&](const LBlock& k) { return k.stage < 0 ? 1 << 30 : k.stage; };
+  std::vector<int64_t> order(nb);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int64_t a, int64_t b) { return srank(B[a]) < srank(B[b]); });
+
+  // ---- slot wiring (bfstructs.jl:107-143)
+  std::unordered_map<SlotKey, int64_t, SlotKeyHash> slot_of;
+  slot_of.reserve((size_t)nb * 2);
+  std::vector<int64_t> slot_len;
+  std::vector<int64_t> in_slot(nb, -1), out_slot(nb, -1);
+  auto get_slot = [&](int32_t bf, int32_t lvl, int64_t o, int64_t s, bool create) -> int64_t {
+    SlotKey key{bf, lvl, o, s};
+    auto it = slot_of.find(key);
+    if (it != slot_of.end()) return it->second;
+    if (!create) return -1;
+    int64_t id = (int64_t)slot_len.size();
+    slot_of.emplace(key, id);
+    slot_len.push_back(-1);
+    return id;
+  };
+  auto node_ok = [&](const ValuesMap& vm, int64_t node) {
+    return node >= 0 && node + 1 < (int64_t)vm.ptr.size();
+  };
+  for (int64_t b : order) {
+    const LBlock& k = B[b];
+    if (k.stage == 0) {
+      if (!node_ok(lg.src_vals, k.si)) {
+        set_error("pack: Q block %lld src_in node %lld unknown", (long long)b, (long long)k.si);
+        return BF_EINVAL;
+      }
+      int64_t m = lg.src_vals.n(k.si);
+      if (!k.ident && k.cols != m) {
+        set_error("pack: Q block %lld has %d cols but values(src_in) has %lld", (long long)b,
+                  k.cols, (long long)m);
+        return BF_EINVAL;
+      }
+      int64_t so = get_slot(k.bf, 0, k.oo, k.so, true);
+      int64_t len = k.ident ? m : k.rows;
+      if (slot_len[so] >= 0 && slot_len[so] != len) {
+        set_error("pack: slot size mismatch at Q block %lld", (long long)b);
+        return BF_EINVAL;
+      }
+      slot_len[so] = len;
+      out_slot[b] = so;
+    } else if (k.stage > 0) {
+      int64_t si = get_slot(k.bf, k.stage - 1, k.oi, k.si, false);
+      if (si < 0 || slot_len[si] < 0) {
+        set_error("pack: R%d block %lld reads a slot no earlier level writes", k.stage,
+                  (long long)b);
+        return BF_EINVAL;
+      }
+      if (!k.ident && k.cols != slot_len[si]) {
+        set_error("pack: R%d block %lld has %d cols, input slot has %lld", k.stage, (long long)b,
+                  k.cols, (long long)slot_len[si]);
+        return BF_EINVAL;
+      }
+      int64_t so = get_slot(k.bf, k.stage, k.oo, k.so, true);
+      int64_t len = k.ident ? slot_len[si] : k.rows;
+      if (slot_len[so] >= 0 && slot_len[so] != len) {
+        set_error("pack: slot size mismatch at R%d block %lld", k.stage, (long long)b);
+        return BF_EINVAL;
+      }
+      slot_len[so] = len;
+      in_slot[b] = si;
+      out_slot[b] = so;
+    } else {
+      int64_t si = get_slot(k.bf, nlev[k.bf] - 1, k.oi, k.si, false);
+      if (si < 0 || slot_len[si] < 0) {
+        set_error("pack: P block %lld reads a slot the last level does not write", (long long)b);
+        return BF_EINVAL;
+      }
+      if (!node_ok(lg.obs_vals, k.oo)) {
+        set_error("pack: P block %lld obs_out node %lld unknown", (long long)b, (long long)k.oo);
+        return BF_EINVAL;
+      }
+      int64_t m = lg.obs_vals.n(k.oo);
+      if (!k.ident && (k.cols != slot_len[si] || k.rows != m)) {
+        set_error("pack: P block %lld is %dx%d, expected %lldx%lld", (long long)b, k.rows, k.cols,
+                  (long long)m, (long long)slot_len[si]);
+        return BF_EINVAL;
+      }
+      if (k.ident && slot_len[si] != m) {
+        set_error("pack: identity P block %lld size mismatch", (long long)b);
+        return BF_EINVAL;
+      }
+      in_slot[b] = si;
+    }
+  }
+  int64_t n_slots = (int64_t)slot_len.size();
+
+  // ---- tasks
+  std::vector<std::vector<TaskB>> stages(Lmax + 1);
+  {  // Q stage: group by source node
+    std::unordered_map<int64_t, int64_t> gid;
+    for (int64_t b : order) {
+      const LBlock& k = B[b];
+      if (k.stage != 0) continue;
+      auto it = gid.find(k.si);
+      if (it == gid.end()) {
+        it = gid.emplace(k.si, (int64_t)stages[0].size()).first;
+        TaskB t;
+        t.stage = 0;
+        t.kind = TASK_DENSE;
+        t.n = lg.src_vals.n(k.si);
+        t.cols.push_back({SIDE_X, k.si, t.n});
+        stages[0].push_back(std::move(t));
+      }
+      TaskB& t = stages[0][it->second];
+      int64_t r = slot_len[out_slot[b]];
+      t.mats.push_back({k.ident ? -1 : b, (int32_t)t.M, 0, k.ident ? (int32_t)t.n : 0});
+      t.rows.push_back({SIDE_SLOT, out_slot[b], r});
+      t.M += r;
+    }
+  }
+  for (int32_t l = 1; l < Lmax; ++l) {  // R levels: connected components over slots
+    std::vector<int64_t> lb;
+    for (int64_t b : order)
+      if (B[b].stage == l) lb.push_back(b);
+    if (lb.empty()) continue;
+    std::unordered_map<int64_t, int64_t> local;  // slot -> dsu index
+    DSU d;
+    auto idx = [&](int64_t slot) {
+      auto it = local.find(slot);
+      if (it != local.end()) return it->second;
+      int64_t i = (int64_t)d.p.size();
+      d.p.push_back(i);
+      local.emplace(slot, i);
+      return i;
+    };
+    for (int64_t b : lb)
+      if (!B[b].ident) d.unite(idx(in_slot[b]), idx(out_slot[b]));
+    std::unordered_map<int64_t, int64_t> comp;  // dsu root -> task
+    std::unordered_map<int64_t, int32_t> row_off, col_off;  // slot -> offset in task
+    for (int64_t b : lb) {
+      const LBlock& k = B[b];
+      if (k.ident) {
+        TaskB t;
+        t.stage = l;
+        t.kind = TASK_COPY;
+        int64_t len = slot_len[in_slot[b]];
+        t.rows.push_back({SIDE_SLOT, out_slot[b], len});
+        t.cols.push_back({SIDE_SLOT, in_slot[b], len});
+        t.M = t.n = len;
+        stages[l].push_back(std::move(t));
+        continue;
+      }
+      int64_t root = d.find(idx(in_slot[b]));
+      auto it = comp.find(root);
+      if (it == comp.end()) {
+        it = comp.emplace(root, (int64_t)stages[l].size()).first;
+        TaskB t;
+        t.stage = l;
+        t.kind = TASK_DENSE;
+        stages[l].push_back(std::move(t));
+      }
+      TaskB& t = stages[l][it->second];
+      if (!row_off.count(out_slot[b])) {
+        row_off[out_slot[b]] = (int32_t)t.M;
+        t.rows.push_back({SIDE_SLOT, out_slot[b], slot_len[out_slot[b]]});
+        t.M += slot_len[out_slot[b]];
+      }
+      if (!col_off.count(in_slot[b])) {
+        col_off[in_slot[b]] = (int32_t)t.n;
+        t.cols.push_back({SIDE_SLOT, in_slot[b], slot_len[in_slot[b]]});
+        t.n += slot_len[in_slot[b]];
+      }
+      t.mats.push_back({b, row_off[out_slot[b]], col_off[in_slot[b]], 0});
+    }
+  }
+  {  // P stage: group by observer node
+    std::unordered_map<int64_t, int64_t> gid;
+    for (int64_t b : order) {
+      const LBlock& k = B[b];
+      if (k.stage >= 0) continue;
+      auto it = gid.find(k.oo);
+      if (it == gid.end()) {
+        it = gid.emplace(k.oo, (int64_t)stages[Lmax].size()).first;
+        TaskB t;
+        t.stage = Lmax;
+        t.kind = TASK_DENSE;
+        t.M = lg.obs_vals.n(k.oo);
+        t.rows.push_back({SIDE_Y, k.oo, t.M});
+        stages[Lmax].push_back(std::move(t));
+      }
+      TaskB& t = stages[Lmax][it->second];
+      int64_t c = slot_len[in_slot[b]];
+      t.mats.push_back({k.ident ? -1 : b, 0, (int32_t)t.n, k.ident ? (int32_t)c : 0});
+      t.cols.push_back({SIDE_SLOT, in_slot[b], c});
+      t.n += c;
+    }
+  }
+  // big tasks first inside each launch (longest-processing-time order)
+  for (auto& st : stages)
+    std::stable_sort(st.begin(), st.end(),
+                     [](const TaskB& a, const TaskB& b) { return a.M * a.n > b.M * b.n; });
+
+  // ---- workspace layout: [x space | y space | slots in reader order]
+  plan.xg_off = 0;
+  plan.yg_off = lg.n_cols;
+  int64_t ws = lg.n_cols + lg.n_rows;
+  std::vector<int64_t> slot_off(n_slots, -1);
+  for (int32_t s = 1; s <= Lmax; ++s)
+    for (auto& t : stages[s])
+      for (auto& c : t.cols)
+        if (c.type == SIDE_SLOT && slot_off[c.id] < 0) {
+          slot_off[c.id] = ws;
+          ws += c.len;
+        }
+  for (int64_t s = 0; s < n_slots; ++s)
+    if (slot_off[s] < 0) {
+      slot_off[s] = ws;
+      ws += std::max<int64_t>(slot_len[s], 0);
+    }
+  plan.ws_entries = ws;
+  if (ws >= (int64_t)1 << 31) {
+    set_error("pack: workspace of %lld entries exceeds int32 routing", (long long)ws);
+    return BF_ENOTSUP;
+  }
+
+  // ---- emit tasks, maps, repack segments
+  std::vector<uint8_t> ycov(lg.n_rows, 0), xcov(lg.n_cols, 0);
+  plan.stage_begin.push_back(0);
+  int64_t a_off = 0;
+  int64_t alg = 0;
+  for (int32_t s = 0; s <= Lmax; ++s) {
+    for (auto& t : stages[s]) {
+      if (t.M > INT32_MAX || t.n > INT32_MAX) {
+        set_error("pack: task too large");
+        return BF_ENOTSUP;
+      }
+      DTask d{};
+      d.M = (int)t.M;
+      d.n = (int)t.n;
+      d.kind = t.kind;
+      d.rmap_off = (long long)plan.maps.size();
+      auto emit = [&](const Side& sd, bool is_row) {
+        if (sd.type == SIDE_SLOT) {
+          for (int64_t i = 0; i < sd.len; ++i) plan.maps.push_back((int32_t)(slot_off[sd.id] + i));
+        } else if (sd.type == SIDE_X) {
+          const int64_t* v = lg.src_vals.v(sd.id);
+          for (int64_t i = 0; i < sd.len; ++i) {
+            plan.maps.push_back((int32_t)(plan.xg_off + v[i]));
+            xcov[v[i]] = 1;
+          }
+        } else {
+          const int64_t* v = lg.obs_vals.v(sd.id);
+          for (int64_t i = 0; i < sd.len; ++i) {
+            plan.maps.push_back((int32_t)(plan.yg_off + v[i]));
+            if (ycov[v[i]]) {
+              set_error("pack: output row %lld written by two P tasks", (long long)v[i]);
+              throw BF_EINVAL;
+            }
+            ycov[v[i]] = 1;
+          }
+        }
+        (void)is_row;
+      };
+      try {
+        for (auto& r : t.rows) emit(r, true);
+        d.cmap_off = (long long)plan.maps.size();
+        for (auto& c : t.cols) emit(c, false);
+      } catch (int code) {
+        return code;
+      }
+      if (t.kind == TASK_DENSE) {
+        d.a_off = a_off;
+        for (auto& m : t.mats) {
+          DSeg g{};
+          g.dst_ld = (int)t.M;
+          g.dst_off = a_off + (long long)m.col_off * t.M + m.row_off;
+          if (m.blk < 0) {
+            g.kind = 1;
+            g.rows = g.cols = m.ident_n;
+            alg += 0;
+          } else {
+            const LBlock& k = B[m.blk];
+            g.kind = 0;
+            g.src_off = k.raw_off;
+            g.src_ld = k.raw_ld;
+            g.rows = k.rows;
+            g.cols = k.cols;
+            plan.block_entries += (int64_t)k.rows * k.cols;
+            plan.max_rank = std::max<int64_t>(plan.max_rank, k.rows);
+          }
+          if (g.rows > 0 && g.cols > 0) plan.segs.push_back(g);
+        }
+        a_off += t.M * t.n;
+      } else {
+        d.a_off = -1;
+      }
+      plan.tasks.push_back(d);
+    }
+    plan.stage_begin.push_back((int64_t)plan.tasks.size());
+  }
+  plan.a_entries = a_off;
+  plan.yg_covered = std::all_of(ycov.begin(), ycov.end(), [](uint8_t c) { return c != 0; });
+  plan.xg_covered = std::all_of(xcov.begin(), xcov.end(), [](uint8_t c) { return c != 0; });
+  int64_t slot_total = 0;
+  for (int64_t s = 0; s < n_slots; ++s) slot_total += std::max<int64_t>(slot_len[s], 0);
+  // algorithmic bytes of one forward matvec (factor entries + x read + y write +
+  // every level slot written once and read once), 16 B per complex entry
+  plan.alg_bytes_fwd = 16 * (plan.block_entries + lg.n_rows + lg.n_cols + 2 * slot_total);
+  (void)alg;
+  return BF_OK;
+}
+
+}  // namespace bfg

@@ -1,0 +1,225 @@
+/*
+ * bfgpu.h -- C ABI of the GB300 far-field butterfly library (libbfgpu.so).
+ *
+ * The library replaces the far-field hot path of ButterflyFactorizations.jl:
+ * the butterfly matvec (forward, adjoint, transpose; one or many right-hand
+ * sides) and the kernel sampling + partial-RRQR skeletonisation that builds the
+ * factors.  Every entry point below names the reference interface it stands in
+ * for (paths relative to the ButterflyFactorizations.jl repository).
+ *
+ * Conventions
+ *   - Plain pointers and sizes only; no exceptions cross the ABI.  Every call
+ *     returns a status code (BF_OK on success); bf_last_error() returns a
+ *     thread-local description of the last failure.
+ *   - Indices are 0-based (the Julia binding subtracts 1).
+ *   - Complex numbers are interleaved (re, im) doubles, i.e. Julia ComplexF64.
+ *   - Matrices of right-hand sides are column-major with a leading dimension.
+ *   - An operator handle owns its device memory and its CUDA stream.  Calls on
+ *     one handle must be serialised by the caller (the reference operator is
+ *     likewise not re-entrant, src/Matrixassembly/matrixstructs.jl:20-21);
+ *     distinct handles are independent.
+ *   - There is no CPU fallback: without a usable CUDA device every compute
+ *     entry point returns BF_ECUDA.
+ */
+#ifndef BFGPU_H
+#define BFGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define BF_API __attribute__((visibility("default")))
+#else
+#define BF_API
+#endif
+
+/* ---- status codes (no reference counterpart: Julia raises exceptions) ---- */
+enum {
+  BF_OK = 0,
+  BF_EINVAL = 1,    /* invalid argument or malformed factor description */
+  BF_ENOMEM = 2,    /* device or host allocation failed                  */
+  BF_ECUDA = 3,     /* CUDA runtime / launch error, or no device          */
+  BF_ETIMEOUT = 4,  /* a bounded device-side wait gave up                 */
+  BF_ENOTSUP = 5,   /* feature not supported for this operator            */
+  BF_ESTATE = 6     /* call not valid in the handle's current state       */
+};
+
+/* ---- operation selector for matvecs ---- */
+enum {
+  BF_OP_N = 0, /* y = beta*y + alpha*A*x            (matrixvector.jl:8-65)        */
+  BF_OP_C = 1, /* y = beta*y + alpha*A'*x (adjoint) (matrix_adj_tr.jl:8-25)       */
+  BF_OP_T = 2  /* y = beta*y + alpha*transpose(A)*x (matrix_adj_tr.jl:28-40)      */
+};
+
+/* ---- pointer-location flags for matvecs ---- */
+enum {
+  BF_PTR_HOST = 0,  /* x, y are host pointers: copies happen inside the call */
+  BF_PTR_DEVICE = 1 /* x, y are device pointers: the call is stream-ordered  */
+};
+
+typedef struct bf_context* bf_ctx_t;
+typedef struct bf_tree* bf_tree_t;
+typedef struct bf_operator* bf_op_t;
+
+BF_API int bf_version(void);
+BF_API const char* bf_status_string(int status);
+BF_API const char* bf_last_error(void);
+
+/* Create / destroy a device context (one CUDA device). */
+BF_API int bf_ctx_create(int device, bf_ctx_t* out);
+BF_API int bf_ctx_destroy(bf_ctx_t ctx);
+
+/* ------------------------------------------------------------------------
+ * Cluster trees (caller-side utility).
+ * A 2^3 tree on the bounding cube of the points: a node is a leaf when it
+ * holds <= max_points points (max_points > 0), or sits at depth max_depth
+ * (max_depth >= 0, root depth 0), or holds one point.  Stands in for the
+ * H2Trees.TwoNTree the reference clusters with (ext/BFH2Trees/BFH2Trees.jl),
+ * exposing the tree contract of src/treeinterface.jl:39-164 as arrays.
+ * values(node) = perm[begin[node] .. end[node]-1].
+ * ------------------------------------------------------------------------ */
+BF_API int bf_tree_build(const double* xyz, int64_t n_points, int32_t max_points,
+                         int32_t max_depth, bf_tree_t* out);
+BF_API int bf_tree_from_arrays(int64_t n_nodes, int64_t n_points, const double* center,
+                               const double* halfsize, const int32_t* parent,
+                               const int32_t* first_child, const int32_t* n_child,
+                               const int64_t* begin, const int64_t* end, const int64_t* perm,
+                               bf_tree_t* out);
+BF_API int bf_tree_size(bf_tree_t tree, int64_t* n_nodes, int64_t* n_points, int32_t* depth);
+BF_API int bf_tree_export(bf_tree_t tree, double* center, double* halfsize, int32_t* level,
+                          int32_t* parent, int32_t* first_child, int32_t* n_child,
+                          int64_t* begin, int64_t* end, int64_t* perm);
+BF_API int bf_tree_destroy(bf_tree_t tree);
+
+/* Near/far interaction lists: src/Matrixassembly/intlists.jl:30-217 with the
+ * AABB isFarFunctor(alpha) of ext/BFH2Trees/h2admissible.jl:11-45 (balanced
+ * splitting).  Call with capacity 0 to query *n_far; pairs are written as
+ * (far_obs[i], far_src[i]) in the reference's depth-first order. */
+BF_API int bf_nearandfar(bf_tree_t obs_tree, bf_tree_t src_tree, double alpha,
+                         int32_t minbflvl, int32_t leafcomp, int32_t leafimbalance,
+                         int64_t* far_obs, int64_t* far_src, int64_t capacity,
+                         int64_t* n_far, int64_t* n_near);
+
+/* ------------------------------------------------------------------------
+ * Construction on the GPU.
+ * Replaces assemble_BF (src/ButterflyFactorization/bfassembly.jl:48-200),
+ * called once per far pair by PetrovGalerkinBF
+ * (src/Matrixassembly/petrovgalerkinbf.jl:129-151), with the PartialQR
+ * compressor (src/ButterflyFactorization/compressors.jl:81-165) and the
+ * ButterflyRankEstimator (src/ButterflyFactorization/rankestimation.jl:93-98).
+ * All far pairs of one operator are built level by level in batched launches
+ * on the point Helmholtz kernel G(r) = exp(-i k r) / (4 pi r).
+ * ------------------------------------------------------------------------ */
+typedef struct {
+  double c_tau;          /* rank-estimator constant Ctau (reference default 4.0;
+                            PetrovGalerkinBF with isFar uses 2.9592)              */
+  int32_t min_samples;   /* lower bound on sampled rows (reference: 10)           */
+  int32_t adaptive;      /* 1 = double the sample while r > floor(0.8 rows)      */
+  uint64_t seed;         /* keys the observer-row sampling                        */
+  int32_t rank_mode;     /* 0 = oversampling estimator; 1 = learned surrogate      */
+  int32_t keep_mixed;    /* 1 = also keep complex-FP32 factors for bf_matvec_mixed */
+  const float* surrogate_weights; /* MLP weights when rank_mode == 1 (else NULL)   */
+  int64_t surrogate_nweights;
+} bf_build_opts;
+
+BF_API void bf_build_opts_default(bf_build_opts* opts);
+
+BF_API int bf_build(bf_ctx_t ctx, const double* obs_xyz, int64_t n_obs, const double* src_xyz,
+                    int64_t n_src, bf_tree_t obs_tree, bf_tree_t src_tree,
+                    const int64_t* far_obs, const int64_t* far_src, int64_t n_far, double k,
+                    double tol, const bf_build_opts* opts, bf_op_t* out);
+
+/* ------------------------------------------------------------------------
+ * Import of factors built elsewhere (the parity path): a set of
+ * ButterflyFactorization objects (src/ButterflyFactorization/bfstructs.jl:21-146)
+ * described block by block.  stage = 0 for Q blocks, l (1-based) for blocks of
+ * R level l, -1 for P blocks.  Keys are the reference routing keys
+ * (obs_out, src_out, obs_in, src_in).  Block data are ComplexF64, column-major
+ * rows x cols, starting at data + 2*data_off[b].  identity[b] != 0 marks a
+ * UniformScaling block (rows/cols/data ignored).  The node->values maps of the
+ * observer (test) and source (trial) trees are CSR arrays: values(node) =
+ * idx[ptr[node] .. ptr[node+1]-1] (0-based point indices).
+ * ------------------------------------------------------------------------ */
+typedef struct {
+  int64_t n_rows, n_cols;
+  int64_t n_blocks;
+  const int32_t* bf;
+  const int32_t* stage;
+  const int64_t* obs_out;
+  const int64_t* src_out;
+  const int64_t* obs_in;
+  const int64_t* src_in;
+  const int32_t* rows;
+  const int32_t* cols;
+  const int8_t* identity;
+  const int64_t* data_off;
+  const double* data;
+  int64_t n_obs_nodes;
+  const int64_t* obs_ptr;
+  const int64_t* obs_idx;
+  int64_t n_src_nodes;
+  const int64_t* src_ptr;
+  const int64_t* src_idx;
+} bf_factor_desc;
+
+BF_API int bf_import_factors(bf_ctx_t ctx, const bf_factor_desc* desc, bf_op_t* out);
+
+/* ------------------------------------------------------------------------
+ * Matvec, FP64-accurate: Y = beta*Y + alpha*op(A)*X over all far blocks.
+ * Replaces mul!(y, A::PetrovGalerkinBF, x, alpha, beta) far part
+ * (src/matrixalgebra/matrixvector.jl:8-65), the per-block flat mul!
+ * (src/Butterflyalgebra/bfvector.jl:200-296) and the multi-RHS column loop
+ * (src/Butterflyalgebra/bfmatrix.jl:10-75).  adjoint/transpose reuse the
+ * forward factors (no copy; cf. src/Butterflyalgebra/bfadjtr.jl:43-67).
+ * x, y: complex (re,im) doubles; alpha, beta: complex scalars as double[2].
+ * stream: a cudaStream_t, or NULL for the handle's own stream.
+ * ------------------------------------------------------------------------ */
+BF_API int bf_matvec(bf_op_t op, int trans, int64_t nrhs, const double* x, int64_t ldx,
+                     double* y, int64_t ldy, const double* alpha, const double* beta,
+                     int ptr_mode, void* stream);
+
+/* Many-RHS mixed precision: factors in complex FP32, split into BF16 hi/lo and
+ * contracted in three tensor-core passes with FP32 accumulation.  Same
+ * arguments as bf_matvec; relative error ~1e-5 instead of ~1e-14. */
+BF_API int bf_matvec_mixed(bf_op_t op, int trans, int64_t nrhs, const double* x, int64_t ldx,
+                           double* y, int64_t ldy, const double* alpha, const double* beta,
+                           int ptr_mode, void* stream);
+
+/* size(A) (src/matrixalgebra/dims.jl:13-20). */
+BF_API int bf_op_size(bf_op_t op, int64_t* n_rows, int64_t* n_cols);
+
+typedef struct {
+  int64_t n_bf;              /* far blocks (butterflies)                        */
+  int64_t n_stages;          /* launches of the level sequence (Q, R..., P)     */
+  int64_t n_tasks;           /* dense + copy tasks over all stages              */
+  int64_t factor_entries;    /* stored complex entries (incl. stacking zeros)   */
+  int64_t factor_bytes;      /* bytes of the FP64-accurate factor array         */
+  int64_t workspace_entries; /* complex entries of the level vectors            */
+  int64_t map_entries;       /* int32 row/column routing entries                */
+  int64_t alg_bytes_fwd;     /* algorithmic bytes of one 1-RHS matvec           */
+  int64_t max_rank;          /* largest block row count                         */
+  double build_seconds;      /* wall time of bf_build (0 for imports)           */
+  int64_t compressions;      /* partial-QR compressions performed               */
+  int64_t retries;           /* adaptive re-samplings                           */
+  int64_t kernel_entries;    /* Helmholtz entries evaluated during the build    */
+} bf_op_stats;
+
+BF_API int bf_op_stats_get(bf_op_t op, bf_op_stats* stats);
+
+/* Copy back the factors as the reference block list (same layout as
+ * bf_factor_desc).  Call with data == NULL to query n_blocks and n_data. */
+BF_API int bf_op_export_blocks(bf_op_t op, int64_t* n_blocks, int64_t* n_data, int32_t* bf,
+                               int32_t* stage, int64_t* obs_out, int64_t* src_out,
+                               int64_t* obs_in, int64_t* src_in, int32_t* rows, int32_t* cols,
+                               int8_t* identity, int64_t* data_off, double* data);
+
+BF_API int bf_op_destroy(bf_op_t op);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BFGPU_H */

@@ -1,0 +1,175 @@
+"""CPU tests of the oracle: it must satisfy the reference's own acceptance criteria.
+
+The reference tests compare butterfly products with dense products at
+``< 10*tol`` (test/test_subroutines.jl:174-182, test/test_prunedtrees.jl:115-116)
+and adjoints at ``< 1e-2`` (test/test_bfadjtr.jl:133-185); here the same
+criteria run on point-Helmholtz geometries.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from bfgpu import geometry as G
+from oracle import bfref as O
+from _util import relerr
+
+TOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def c1():
+    """Plain single block (4,096 x 4,096 plane pair, quadtree depth 4, lambda = 0.125)."""
+    obs, src = G.plane_pair(4096, seed=1)
+    k = 2 * math.pi / 0.125
+    to = O.build_tree(obs, max_depth=4)
+    ts = O.build_tree(src, max_depth=4)
+    kern = O.HelmholtzKernel(obs, src, k)
+    log = []
+    bf = O.assemble_bf(kern, to, ts, 0, 0, k, TOL, c_tau=4.0, seed=3, log=log)
+    return dict(obs=obs, src=src, k=k, to=to, ts=ts, kern=kern, bf=bf, log=log)
+
+
+def test_sample_positions_is_permutation():
+    for n in [1, 2, 3, 7, 16, 17, 100, 1000, 4097]:
+        for key in [0, 1, 0xDEADBEEF, (1 << 64) - 1]:
+            p = O.sample_positions(0, n, n, key)
+            assert sorted(p.tolist()) == list(range(n))
+            # prefix / extension property used by the adaptive retry
+            q = np.concatenate([O.sample_positions(0, n // 3, n, key),
+                                O.sample_positions(n // 3, n, n, key)])
+            assert np.array_equal(p, q)
+
+
+def test_task_key_matches_reference_constants():
+    # SplitMix64 finaliser of 0 (published SplitMix64 first output for seed 0)
+    assert O.mix64(0) == 0xE220A8397B1DCDAF
+    assert O.task_key(0, 1, 2) != O.task_key(0, 2, 1)
+
+
+def test_pqr_truncation_and_interpolation():
+    rng = np.random.default_rng(0)
+    m, n, r = 60, 80, 12
+    U = rng.standard_normal((m, r)) + 1j * rng.standard_normal((m, r))
+    V = rng.standard_normal((r, n)) + 1j * rng.standard_normal((r, n))
+    Z = U @ V + 1e-9 * (rng.standard_normal((m, n)) + 1j * rng.standard_normal((m, n)))
+
+    def kern(rows, cols):
+        return Z[np.ix_(rows, cols)]
+
+    T, skel, rank = O.partial_qr(kern, np.arange(n), np.arange(m), 40, 1e-6, True, key=5)
+    assert rank == r
+    assert T.shape == (r, n)
+    assert relerr(Z[:, skel] @ T, Z) < 1e-7
+    # interpolation matrix is the identity on the skeleton columns
+    assert np.allclose(T[:, skel], np.eye(r), atol=1e-8)
+
+
+def test_traverseandpad_drops_leaves_to_bottom():
+    # src/auxillaries.jl:340-350; test/test_auxillaries.jl:116-124
+    pts = G.cube_surface(3000, seed=2)
+    t = O.build_tree(pts, max_points=40)
+    lv = O.traverseandpad(t, 0)
+    leaves = set(np.nonzero(t.n_child == 0)[0].tolist())
+    assert set(lv[-1]) == leaves
+    raw = O.treelevels(t, 0)
+    for a, b in zip(lv, raw):
+        assert b == a[:len(b)]
+
+
+def test_nearandfar_partitions_the_matrix():
+    pts = G.fibonacci_sphere(1500)
+    t = O.build_tree(pts, max_points=24)
+    far, near = O.nearandfar(t, t, alpha=1.0)
+    cover = np.zeros((1500, 1500), np.int32)
+    for o, s in far + near:
+        cover[np.ix_(t.values(o), t.values(s))] += 1
+    assert cover.min() == 1 and cover.max() == 1
+    assert all(O.is_far(t, t, s, o, 1.0) for o, s in far)
+
+
+def test_c1_matches_dense_within_10_tol(c1):
+    n = 4096
+    A = c1["kern"](np.arange(n), np.arange(n))
+    x = G.complex_gaussian(n, 7)
+    y = O.matvec_flat(c1["bf"], x, np.zeros(n, complex))
+    assert relerr(y, A @ x) < 10 * TOL
+    assert len(c1["log"]) == 1280  # 256 Q + 4 levels x 256 R compressions
+
+
+def test_flat_and_dict_orders_agree(c1):
+    x = G.complex_gaussian(4096, 8)
+    y1 = O.matvec_flat(c1["bf"], x, np.zeros(4096, complex))
+    y2 = O.matvec_dict(c1["bf"], x, np.zeros(4096, complex))
+    assert relerr(y1, y2) < 1e-14
+
+
+def test_alpha_beta_semantics(c1):
+    x = G.complex_gaussian(4096, 9)
+    y0 = G.complex_gaussian(4096, 10)
+    ref = O.matvec_flat(c1["bf"], x, np.zeros(4096, complex))
+    y = y0.copy()
+    O.matvec_flat(c1["bf"], x, y, alpha=2 - 1j, beta=0.5j)
+    assert relerr(y, 0.5j * y0 + (2 - 1j) * ref) < 1e-14
+
+
+def test_adjoint_and_transpose_match_dense(c1):
+    n = 4096
+    A = c1["kern"](np.arange(n), np.arange(n))
+    v = G.complex_gaussian(n, 11)
+    ya = O.matvec_flat(O.adjoint_bf(c1["bf"], "C"), v, np.zeros(n, complex))
+    yt = O.matvec_flat(O.adjoint_bf(c1["bf"], "T"), v, np.zeros(n, complex))
+    assert relerr(ya, A.conj().T @ v) < 10 * TOL
+    assert relerr(yt, A.T @ v) < 10 * TOL
+
+
+@pytest.mark.parametrize("deep_obs", [True, False])
+def test_unbalanced_trees_match_dense(deep_obs):
+    # test/test_subroutines.jl:46-54 (deep observer / shallow source and back)
+    obs, src = G.plane_pair(1500, seed=4, z_obs=2.5)
+    k = 2 * math.pi / 0.25
+    to = O.build_tree(obs, max_points=12 if deep_obs else 200)
+    ts = O.build_tree(src, max_points=200 if deep_obs else 12)
+    kern = O.HelmholtzKernel(obs, src, k)
+    bf = O.assemble_bf(kern, to, ts, 0, 0, k, TOL, seed=1)
+    assert (len(O.traverseandpad(to, 0)) != len(O.traverseandpad(ts, 0)))
+    x = G.complex_gaussian(1500, 1)
+    A = kern(np.arange(1500), np.arange(1500))
+    y = O.matvec_flat(bf, x, np.zeros(1500, complex))
+    assert relerr(y, A @ x) < 10 * TOL
+    ya = O.matvec_flat(O.adjoint_bf(bf), x, np.zeros(1500, complex))
+    assert relerr(ya, A.conj().T @ x) < 10 * TOL
+
+
+def test_global_far_operator_matches_dense():
+    n = 2500
+    pts = G.fibonacci_sphere(n)
+    k = G.wavenumber(n, 4 * math.pi)
+    t = O.build_tree(pts, max_points=24)
+    kern = O.HelmholtzKernel(pts, pts, k)
+    op = O.assemble_far(kern, t, t, k, TOL)
+    D = O.dense_far(kern, op)
+    x = G.complex_gaussian(n, 3)
+    y = O.far_matvec(op, x)
+    assert relerr(y, D @ x) < 10 * TOL
+    ya = O.far_matvec(op, x, adjoint=True)
+    assert relerr(ya, D.conj().T @ x) < 10 * TOL
+
+
+@pytest.mark.parametrize("name", ["plane_single", "plane_unbalanced", "sphere_far"])
+def test_oracle_reproduces_golden_fixtures(name):
+    import importlib.util
+    import os
+    from _util import oracle_blocks
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(here, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    far, _, _ = mg.build(name)
+    g = np.load(os.path.join(here, f"{name}.npz"))
+    d = oracle_blocks(far.bfs)
+    for key in ["bf", "stage", "obs_out", "src_out", "obs_in", "src_in", "rows", "cols",
+                "identity", "data_off"]:
+        assert np.array_equal(d[key], g[key]), key
+    assert relerr(d["data"], g["data"]) < 1e-12
+    assert relerr(O.far_matvec(far, g["x"]), g["y"]) < 1e-12
