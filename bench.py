@@ -1,0 +1,355 @@
+#!/usr/bin/env python
+"""Far-field butterfly matvec throughput on GB300.
+
+Default workload (one GPU): the plain FP64 far-field operator of a
+65,536-point Fibonacci sphere at ~100 points per wavelength^2 (k ~ 45.4),
+octree with <= 32 points per leaf, isFar(alpha=1) admissibility, tol 1e-4,
+one complex Gaussian right-hand side.  Factors are built on the GPU by
+bf_build before timing; a step is one forward far-field matvec over all
+653,570 butterflies.  The factor stream (~10 GB) is far larger than L2, so no
+explicit L2 flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs independent replicas (one per rank, launched by torch.distributed.run);
+the path has no cross-GPU exchange on a single operator.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path[:0] = [ROOT, os.path.join(ROOT, "butterflyfactorizations.jl_gb300")]
+
+import numpy as np  # noqa: E402
+
+METRIC = "far-field matvecs/s & HBM GB/s: plain FP64 vs batched mixed, rel.err≤1e-4"
+UNIT = "matvec/s"
+
+WORKLOADS = {
+    # name: (n points, max points per leaf, tol)
+    "sphere65k": (65536, 32, 1e-4),
+    "sphere16k": (16384, 32, 1e-4),
+    "sphere4k": (4096, 32, 1e-4),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="sphere65k")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    return ap.parse_args()
+
+
+def dist_setup(n_gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(v, world):
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def build_workload(name, device):
+    import bfgpu
+    from bfgpu import geometry as G
+    n, leaf, tol = WORKLOADS[name]
+    pts = G.fibonacci_sphere(n)
+    k = G.wavenumber(n, 4.0 * math.pi)
+    tree = bfgpu.Tree.build(pts, max_points=leaf)
+    far, n_near = bfgpu.nearandfar(tree, tree, 1.0)
+    ctx = bfgpu.Context(device)
+    t0 = time.perf_counter()
+    op = bfgpu.PetrovGalerkinBF(pts, pts, tree, tree, k, tol=tol, ctx=ctx)
+    build_s = time.perf_counter() - t0
+    x = G.complex_gaussian(n, 1234)
+    return dict(pts=pts, k=k, tree=tree, far=far, n_near=n_near, ctx=ctx, op=op, x=x, n=n,
+                tol=tol, build_s=build_s)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = max(mx, float(r[2]))
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def committed_traffic(workload):
+    """DRAM bytes per launch of the dominant stage from a committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "stage_traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d.get(workload)
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_baseline(w, reps=3):
+    """Reference flat matvec (oracle C port, OpenMP) on the same factors."""
+    from oracle.cbind import CRefOperator
+    op = w["op"]
+    ex = op.export_blocks()
+    csr = w["tree"].values_csr()
+    cref = CRefOperator(w["n"], w["n"], ex, csr, csr)
+    del ex
+    threads = os.cpu_count() or 1
+    x = w["x"]
+    y = cref.matvec(x, nthreads=threads)  # warm-up (page-in)
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        cref.matvec(x, y, nthreads=threads)
+        ts.append(time.perf_counter() - t0)
+    t = statistics.median(ts)
+    return dict(value=1.0 / t, unit=UNIT, cores=threads, kind="port",
+                sample=f"full far-field matvec ({w['op'].stats()['n_bf']} butterflies, "
+                       f"ComplexF64 factors), median of {reps} after 1 warm-up, "
+                       f"{threads} OpenMP threads"), y
+
+
+def run_reference(args, rank, world, local):
+    if rank != 0:
+        return
+    w = build_workload(args.workload, local)
+    from oracle.cbind import CRefOperator
+    ex = w["op"].export_blocks()
+    csr = w["tree"].values_csr()
+    cref = CRefOperator(w["n"], w["n"], ex, csr, csr)
+    del ex
+    threads = os.cpu_count() or 1
+    x = w["x"]
+    y = np.zeros(w["n"], np.complex128)
+    for _ in range(args.warmup):
+        cref.matvec(x, y, nthreads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cref.matvec(x, y, nthreads=threads)
+    dt = (time.perf_counter() - t0) / args.steps
+    v = 1.0 / dt
+    st = w["op"].stats()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"{args.workload}: Fibonacci sphere N={w['n']}, k={w['k']:.2f}, "
+                               f"octree<=32/leaf, isFar(1.0), tol={w['tol']}, 1 RHS",
+                   "global_batch": 1, "n_far": st["n_bf"], "parallelism": "cpu-openmp"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "full far-field matvec per step; factors built by bf_build "
+                                   "and exported as ComplexF64 (the timed code is the C "
+                                   "restatement of bfvector.jl:200-296 + matrixvector.jl:8-65)"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    import bfgpu
+    torch.cuda.set_device(local)
+    w = build_workload(args.workload, local)
+    op = w["op"]
+    n = w["n"]
+    st = op.stats()
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    xd = torch.from_numpy(w["x"]).to(f"cuda:{local}")
+    yd = torch.zeros_like(xd)
+
+    def step():
+        op.matvec_ptr(xd.data_ptr(), n, yd.data_ptr(), n, ptr_mode=bfgpu.BF_PTR_DEVICE, stream=sp)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    clk = ClockSampler(local)
+    clk.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    ms = max_over_ranks(ms, world)
+    value = world * 1000.0 / ms
+
+    # accuracy of this step against sampled dense far-field rows (FP64 sums)
+    y = yd.cpu().numpy()
+
+    # adjoint throughput (same timing method)
+    opa = op.adjoint()
+
+    def astep():
+        opa.matvec_ptr(xd.data_ptr(), n, yd.data_ptr(), n, ptr_mode=bfgpu.BF_PTR_DEVICE, stream=sp)
+
+    for _ in range(3):
+        astep()
+    e0.record(stream)
+    for _ in range(args.steps):
+        astep()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_adj = e0.elapsed_time(e1) / args.steps
+
+    # e2e through the public C ABI with pinned host buffers (copies inside the call)
+    xh = torch.from_numpy(w["x"]).pin_memory()
+    yh = torch.zeros_like(xh).pin_memory()
+    for _ in range(3):
+        op.matvec_ptr(xh.data_ptr(), n, yh.data_ptr(), n, ptr_mode=bfgpu.BF_PTR_HOST)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        op.matvec_ptr(xh.data_ptr(), n, yh.data_ptr(), n, ptr_mode=bfgpu.BF_PTR_HOST)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e_s = max_over_ranks(e2e_s, world)
+
+    # roofline of the dominant level launch (CUDA events inside the library)
+    stage_ms, stage_bytes, kernels = op.profile(nrep=5)
+    dom = int(np.argmax(stage_ms))
+    achieved = stage_bytes[dom] / (stage_ms[dom] * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    traffic = committed_traffic(args.workload)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 (float-float on FP32 pipes)", "data": "synthetic",
+        "config": {
+            "workload": f"{args.workload}: Fibonacci sphere N={n}, k={w['k']:.2f}, "
+                        f"octree<=32/leaf, isFar(1.0), tol={w['tol']}, 1 complex Gaussian RHS",
+            "global_batch": world, "n_far": st["n_bf"], "parallelism": f"replicas x{world}",
+            "l2": "no flush: factor stream per step > L2 (129 MB)",
+            "factor_bytes": st["factor_bytes"], "alg_bytes_per_matvec": st["alg_bytes_fwd"],
+            "build_seconds": round(w["build_s"], 3), "compressions": st["compressions"],
+            "retries": st["retries"]},
+        "hbm_gbs": st["alg_bytes_fwd"] / (ms * 1e-3) / 1e9,
+        "adjoint": {"value": world * 1000.0 / ms_adj, "unit": UNIT, "ms_per_step": ms_adj,
+                    "hbm_gbs": st["alg_bytes_fwd"] / (ms_adj * 1e-3) / 1e9},
+        "e2e": {"value": world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 16 * n,
+                "d2h_bytes_per_step": 16 * n},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": f"level launch {dom} of {len(stage_ms)} "
+                               f"({'Q' if dom == 0 else 'P' if dom == len(stage_ms) - 1 else 'R'}"
+                               f" stage), {stage_ms[dom]:.3f} ms",
+                     "peak_source": f"{peak_kind} hbm_gbs",
+                     "stage_ms": [round(float(v), 4) for v in stage_ms],
+                     "stage_bytes": [int(v) for v in stage_bytes]},
+        "gpu_launches": int(kernels * args.steps),
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu:
+        try:
+            cb, ycpu = cpu_baseline(w)
+            line["cpu_baseline"] = cb
+            line["parity_vs_cpu_port"] = float(np.linalg.norm(y - ycpu) / np.linalg.norm(ycpu))
+        except Exception as e:  # report, do not fail the GPU measurement
+            line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": 0, "kind": "port",
+                                    "sample": f"failed: {e}"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world, local)
+    else:
+        run_ours(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

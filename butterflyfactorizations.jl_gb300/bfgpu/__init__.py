@@ -226,30 +226,66 @@ class Operator:
                  int(ldy), a, b, BF_PTR_DEVICE, C.c_void_p(stream) if stream else None),
               "bf_matvec(device)")
 
+    def matvec_ptr(self, x_ptr: int, ldx: int, y_ptr: int, ldy: int, nrhs: int = 1,
+                   alpha=1.0, beta=0.0, ptr_mode: int = BF_PTR_HOST, stream: int = 0,
+                   mixed: bool = False):
+        """Raw-pointer matvec; ptr_mode BF_PTR_HOST copies x/y inside the call."""
+        lib = load()
+        a = (C.c_double * 2)(complex(alpha).real, complex(alpha).imag)
+        b = (C.c_double * 2)(complex(beta).real, complex(beta).imag)
+        fn = lib.bf_matvec_mixed if mixed else lib.bf_matvec
+        check(fn(self._h, self.trans, int(nrhs), C.c_void_p(x_ptr), int(ldx), C.c_void_p(y_ptr),
+                 int(ldy), a, b, int(ptr_mode), C.c_void_p(stream) if stream else None),
+              "bf_matvec(ptr)")
+
     def __matmul__(self, x):
         return self.matvec(x)
 
-    def export_blocks(self):
-        """Factors as reference-style block arrays (see ``bf_op_export_blocks``)."""
+    def export_blocks(self, bf_begin: int = 0, bf_end: int | None = None,
+                      as_float32: bool = False):
+        """Factors of far blocks [bf_begin, bf_end) as reference-style block arrays."""
         lib = load()
+        if bf_end is None:
+            bf_end = self.stats()["n_bf"]
         nb, nd = C.c_int64(), C.c_int64()
         N = None
-        check(lib.bf_op_export_blocks(self._h, C.byref(nb), C.byref(nd), *([N] * 11)), "export")
+        check(lib.bf_op_export_blocks(self._h, bf_begin, bf_end, C.byref(nb), C.byref(nd),
+                                      *([N] * 11), 0), "export")
         n = nb.value
         out = dict(bf=np.zeros(n, np.int32), stage=np.zeros(n, np.int32),
                    obs_out=np.zeros(n, np.int64), src_out=np.zeros(n, np.int64),
                    obs_in=np.zeros(n, np.int64), src_in=np.zeros(n, np.int64),
                    rows=np.zeros(n, np.int32), cols=np.zeros(n, np.int32),
                    identity=np.zeros(n, np.int8), data_off=np.zeros(n, np.int64),
-                   data=np.zeros(max(nd.value, 1), np.complex128))
+                   data=np.zeros(max(nd.value, 1), np.complex64 if as_float32 else np.complex128))
         check(lib.bf_op_export_blocks(
-            self._h, C.byref(nb), C.byref(nd), _p(out["bf"], C.c_int32), _p(out["stage"], C.c_int32),
-            _p(out["obs_out"], C.c_int64), _p(out["src_out"], C.c_int64),
-            _p(out["obs_in"], C.c_int64), _p(out["src_in"], C.c_int64),
-            _p(out["rows"], C.c_int32), _p(out["cols"], C.c_int32), _p(out["identity"], C.c_int8),
-            _p(out["data_off"], C.c_int64), out["data"].ctypes.data_as(C.POINTER(C.c_double))),
-            "export")
+            self._h, bf_begin, bf_end, C.byref(nb), C.byref(nd), _p(out["bf"], C.c_int32),
+            _p(out["stage"], C.c_int32), _p(out["obs_out"], C.c_int64),
+            _p(out["src_out"], C.c_int64), _p(out["obs_in"], C.c_int64),
+            _p(out["src_in"], C.c_int64), _p(out["rows"], C.c_int32), _p(out["cols"], C.c_int32),
+            _p(out["identity"], C.c_int8), _p(out["data_off"], C.c_int64),
+            C.c_void_p(out["data"].ctypes.data), int(as_float32)), "export")
         return out
+
+    def rank_log(self) -> np.ndarray:
+        """Per-compression rank records of the build, (n, 14) float64 (see bfgpu.h)."""
+        lib = load()
+        n = C.c_int64()
+        check(lib.bf_op_rank_log(self._h, C.byref(n), None), "rank_log")
+        rec = np.zeros((max(n.value, 1), 14))
+        check(lib.bf_op_rank_log(self._h, C.byref(n), _p(rec, C.c_double)), "rank_log")
+        return rec[:n.value]
+
+    def profile(self, nrep: int = 5):
+        """Per-level launch times (ms), algorithmic bytes and kernels per matvec."""
+        lib = load()
+        ns = self.stats()["n_stages"]
+        ms = np.zeros(ns)
+        by = np.zeros(ns, np.int64)
+        nk = C.c_int64()
+        check(lib.bf_op_profile(self._h, self.trans, int(nrep), _p(ms, C.c_double),
+                                _p(by, C.c_int64), C.byref(nk)), "bf_op_profile")
+        return ms, by, nk.value
 
     def close(self):
         if self._parent is None and self._h and self._h.value:

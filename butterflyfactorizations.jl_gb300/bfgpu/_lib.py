@@ -62,9 +62,11 @@ SIGNATURES = [
                                   vp]),
     ("bf_op_size", C.c_int, [vp, P(i64), P(i64)]),
     ("bf_op_stats_get", C.c_int, [vp, P(OpStats)]),
-    ("bf_op_export_blocks", C.c_int, [vp, P(i64), P(i64), P(i32), P(i32), P(i64), P(i64),
-                                      P(i64), P(i64), P(i32), P(i32), P(C.c_int8), P(i64),
-                                      P(f64)]),
+    ("bf_op_export_blocks", C.c_int, [vp, i64, i64, P(i64), P(i64), P(i32), P(i32), P(i64),
+                                      P(i64), P(i64), P(i64), P(i32), P(i32), P(C.c_int8),
+                                      P(i64), vp, i32]),
+    ("bf_op_rank_log", C.c_int, [vp, P(i64), P(f64)]),
+    ("bf_op_profile", C.c_int, [vp, C.c_int, i32, P(f64), P(i64), P(i64)]),
     ("bf_op_destroy", C.c_int, [vp]),
 ]
 

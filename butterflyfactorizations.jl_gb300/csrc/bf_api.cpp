@@ -24,12 +24,6 @@ const char* last_error() { return g_err; }
 
 using namespace bfg;
 
-struct bf_context {
-  Context c;
-};
-struct bf_operator {
-  Operator op;
-};
 
 #define BF_GUARD_BEGIN try {
 #define BF_GUARD_END                                        \
@@ -252,10 +246,11 @@ int bf_op_stats_get(bf_op_t op, bf_op_stats* st) {
   return BF_OK;
 }
 
-int bf_op_export_blocks(bf_op_t h, int64_t* n_blocks, int64_t* n_data, int32_t* bf,
-                        int32_t* stage, int64_t* obs_out, int64_t* src_out, int64_t* obs_in,
-                        int64_t* src_in, int32_t* rows, int32_t* cols, int8_t* identity,
-                        int64_t* data_off, double* data) {
+int bf_op_export_blocks(bf_op_t h, int64_t bf_begin, int64_t bf_end, int64_t* n_blocks,
+                        int64_t* n_data, int32_t* bf, int32_t* stage, int64_t* obs_out,
+                        int64_t* src_out, int64_t* obs_in, int64_t* src_in, int32_t* rows,
+                        int32_t* cols, int8_t* identity, int64_t* data_off, void* data,
+                        int32_t as_float32) {
   BF_GUARD_BEGIN
   if (!h || !n_blocks || !n_data) {
     set_error("bf_op_export_blocks: NULL argument");
@@ -263,10 +258,13 @@ int bf_op_export_blocks(bf_op_t h, int64_t* n_blocks, int64_t* n_data, int32_t* 
   }
   Operator& op = h->op;
   const auto& B = op.logical.blocks;
-  int64_t tot = 0;
-  for (const auto& k : B)
+  int64_t tot = 0, nb = 0;
+  for (const auto& k : B) {
+    if (k.bf < bf_begin || k.bf >= bf_end) continue;
+    ++nb;
     if (!k.ident) tot += (int64_t)k.rows * k.cols;
-  *n_blocks = (int64_t)B.size();
+  }
+  *n_blocks = nb;
   *n_data = tot;
   if (!data) return BF_OK;
   if (!bf || !stage || !obs_out || !src_out || !obs_in || !src_in || !rows || !cols ||
@@ -279,42 +277,96 @@ int bf_op_export_blocks(bf_op_t h, int64_t* n_blocks, int64_t* n_data, int32_t* 
     return BF_ESTATE;
   }
   BF_TRY_CUDA(cudaSetDevice(op.ctx->device));
-  size_t esz = op.raw_is_double ? 16 : 8;
+  const size_t esz = op.raw_is_double ? 16 : 8;
+  // one bulk copy of the raw store, then a host-side gather per block
   std::vector<char> raw((size_t)op.raw_entries * esz);
-  BF_TRY_CUDA(cudaMemcpy(raw.data(), op.d_raw, raw.size(), cudaMemcpyDeviceToHost));
-  int64_t off = 0;
+  if (!raw.empty())
+    BF_TRY_CUDA(cudaMemcpy(raw.data(), op.d_raw, raw.size(), cudaMemcpyDeviceToHost));
+  int64_t off = 0, ob = 0;
   for (size_t b = 0; b < B.size(); ++b) {
     const LBlock& k = B[b];
-    bf[b] = k.bf;
-    stage[b] = k.stage;
-    obs_out[b] = k.oo;
-    src_out[b] = k.so;
-    obs_in[b] = k.oi;
-    src_in[b] = k.si;
-    rows[b] = k.rows;
-    cols[b] = k.cols;
-    identity[b] = k.ident;
-    data_off[b] = off;
-    if (k.ident) continue;
-    for (int32_t j = 0; j < k.cols; ++j)
-      for (int32_t i = 0; i < k.rows; ++i) {
-        size_t src = (size_t)(k.raw_off + (int64_t)j * k.raw_ld + i);
-        double re, im;
-        if (op.raw_is_double) {
-          const double* p = (const double*)raw.data() + 2 * src;
-          re = p[0];
-          im = p[1];
-        } else {
-          const float* p = (const float*)raw.data() + 2 * src;
-          re = p[0];
-          im = p[1];
-        }
-        data[2 * (off + (int64_t)j * k.rows + i)] = re;
-        data[2 * (off + (int64_t)j * k.rows + i) + 1] = im;
+    if (k.bf < bf_begin || k.bf >= bf_end) continue;
+    bf[ob] = k.bf;
+    stage[ob] = k.stage;
+    obs_out[ob] = k.oo;
+    src_out[ob] = k.so;
+    obs_in[ob] = k.oi;
+    src_in[ob] = k.si;
+    rows[ob] = k.rows;
+    cols[ob] = k.cols;
+    identity[ob] = k.ident;
+    data_off[ob] = off;
+    ++ob;
+    if (k.ident || k.rows * (int64_t)k.cols == 0) continue;
+    size_t ncol = (size_t)k.cols, nrow = (size_t)k.rows;
+    for (size_t e = 0; e < ncol * nrow; ++e) {
+      size_t j = e / nrow, i = e - j * nrow;
+      size_t src = (size_t)k.raw_off + j * (size_t)k.raw_ld + i;
+      double re, im;
+      if (op.raw_is_double) {
+        const double* p = (const double*)raw.data() + 2 * src;
+        re = p[0];
+        im = p[1];
+      } else {
+        const float* p = (const float*)raw.data() + 2 * src;
+        re = p[0];
+        im = p[1];
       }
+      if (as_float32) {
+        ((float*)data)[2 * (off + e)] = (float)re;
+        ((float*)data)[2 * (off + e) + 1] = (float)im;
+      } else {
+        ((double*)data)[2 * (off + e)] = re;
+        ((double*)data)[2 * (off + e) + 1] = im;
+      }
+    }
     off += (int64_t)k.rows * k.cols;
   }
   return BF_OK;
+  BF_GUARD_END
+}
+
+int bf_op_rank_log(bf_op_t h, int64_t* n_rec, double* rec) {
+  if (!h || !n_rec) {
+    set_error("bf_op_rank_log: NULL argument");
+    return BF_EINVAL;
+  }
+  const auto& L = h->op.rank_log;
+  *n_rec = (int64_t)L.size();
+  if (!rec) return BF_OK;
+  for (size_t i = 0; i < L.size(); ++i) {
+    const auto& r = L[i];
+    double* o = rec + 14 * i;
+    o[0] = r.bf;
+    o[1] = r.stage;
+    o[2] = (double)r.obs_node;
+    o[3] = (double)r.src_node;
+    o[4] = r.n_obs;
+    o[5] = r.n_cols;
+    o[6] = r.rows0;
+    o[7] = r.rows;
+    o[8] = r.retries;
+    o[9] = r.rank;
+    o[10] = r.a_obs;
+    o[11] = r.a_src;
+    o[12] = r.dist;
+    o[13] = r.k;
+  }
+  return BF_OK;
+}
+
+int bf_op_profile(bf_op_t h, int trans, int32_t nrep, double* ms_per_stage,
+                  int64_t* bytes_per_stage, int64_t* kernels_per_matvec) {
+  BF_GUARD_BEGIN
+  if (!h) {
+    set_error("bf_op_profile: NULL operator");
+    return BF_EINVAL;
+  }
+  if (trans != BF_OP_N && trans != BF_OP_C && trans != BF_OP_T) {
+    set_error("bf_op_profile: invalid trans");
+    return BF_EINVAL;
+  }
+  return profile_matvec(h->op, trans, nrep, ms_per_stage, bytes_per_stage, kernels_per_matvec);
   BF_GUARD_END
 }
 

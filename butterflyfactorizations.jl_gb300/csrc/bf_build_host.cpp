@@ -1,0 +1,773 @@
+// Host orchestration of the batched GPU construction (bf_build).
+//
+// Restates assemble_BF (src/ButterflyFactorization/bfassembly.jl:48-200) for
+// all far pairs of an operator at once: the Q stage, every R level and the P
+// stage are each one batch of compressions (or dense kernel blocks) executed by
+// the kernels of bf_build.cu.  The host keeps only integer bookkeeping: the
+// padded level lists, the skeleton map K (bfassembly.jl:76-77) and the block
+// keys; matrices never leave the device.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+#include <unordered_map>
+
+#include "bf_build.h"
+#include "bf_surrogate.h"
+
+namespace bfg {
+namespace {
+
+uint64_t mix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// task_key(seed, bf, stage, obs_node, src_node) -- same chain as the oracle
+uint64_t task_key(uint64_t seed, int64_t bf, int64_t stage, int64_t o, int64_t s) {
+  uint64_t h = mix64(seed);
+  h = mix64(h ^ (uint64_t)bf);
+  h = mix64(h ^ (uint64_t)stage);
+  h = mix64(h ^ (uint64_t)o);
+  h = mix64(h ^ (uint64_t)s);
+  return h;
+}
+
+struct KKey {
+  int32_t bf;
+  int64_t s, o;
+  bool operator==(const KKey& k) const { return bf == k.bf && s == k.s && o == k.o; }
+};
+struct KKeyHash {
+  size_t operator()(const KKey& k) const {
+    return (size_t)mix64((uint64_t)k.bf * 0x9E3779B97F4A7C15ull ^ mix64((uint64_t)k.s) ^
+                         ((uint64_t)k.o << 1));
+  }
+};
+struct SkelRef {
+  int64_t off = 0;
+  int32_t len = 0;
+};
+
+struct BFState {
+  int64_t no, ns;
+  std::vector<std::vector<int64_t>> tS, tO;
+  int32_t LS, LO, L;
+  double eps;
+  int32_t n_est;
+};
+
+struct HTask {
+  int32_t bf, stage;
+  int64_t obs_node, src_node;
+  int64_t obs_begin;
+  int32_t n_obs;
+  int64_t cols_off;
+  int32_t n_cols;
+  uint64_t key;
+  double eps;
+  int32_t rows0, rows, retries, rank;
+  int64_t t_off;
+  SkelRef skel;
+};
+
+struct Item {
+  int32_t kind;  // 0 = compression, 1 = identity
+  int32_t bf;
+  int64_t oo, so, oi, si;
+  int64_t split_svert;  // >= 0: split T columns by children of this source node
+  int64_t upd_s, upd_o;
+  int64_t task;
+  SkelRef copy;
+};
+
+template <typename T>
+int dev_reserve(T*& p, int64_t& cap, int64_t need) {
+  if (need <= cap) return BF_OK;
+  if (p) cudaFree(p);
+  p = nullptr;
+  cap = 0;
+  int64_t n = std::max<int64_t>(need, 1024);
+  n += n / 4;
+  if (cudaMalloc(&p, (size_t)n * sizeof(T)) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("build: cannot allocate %lld device entries", (long long)n);
+    return BF_ENOMEM;
+  }
+  cap = n;
+  return BF_OK;
+}
+
+class Builder {
+ public:
+  Builder(Context* ctx, const Tree& to, const Tree& ts, double k, double tol,
+          const bf_build_opts& opts, Operator& op)
+      : ctx_(ctx), to_(to), ts_(ts), k_(k), tol_(tol), opts_(opts), op_(op) {}
+  ~Builder() {
+    for (void* p : {(void*)d_obs_, (void*)d_src_, (void*)d_obs_perm_, (void*)d_colpool_,
+                    (void*)d_ctask_, (void*)d_Z_, (void*)d_rowpool_, (void*)d_permpool_,
+                    (void*)d_skel_})
+      if (p) cudaFree(p);
+  }
+
+  int run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, int64_t n_src,
+          const int64_t* far_obs, const int64_t* far_src, int64_t n_far);
+
+ private:
+  int ensure_raw(int64_t need);
+  int run_compressions(std::vector<HTask>& tasks, const std::vector<int32_t>& colpool);
+  int run_dense(std::vector<HTask>& tasks, const std::vector<int32_t>& colpool);
+  void add_values(std::vector<int32_t>& pool, const Tree& t, int64_t node) {
+    const int64_t* v = t.vals(node);
+    for (int64_t i = 0; i < t.nvals(node); ++i) pool.push_back((int32_t)v[i]);
+  }
+  void add_skel(std::vector<int32_t>& pool, const SkelRef& r) {
+    pool.insert(pool.end(), skel_.begin() + r.off, skel_.begin() + r.off + r.len);
+  }
+  HTask make_task(int32_t f, int32_t stage, int64_t obs_node, int64_t src_node, int64_t cols_off,
+                  int32_t n_cols) {
+    const BFState& st = bfs_[f];
+    HTask t{};
+    t.bf = f;
+    t.stage = stage;
+    t.obs_node = obs_node;
+    t.src_node = src_node;
+    t.obs_begin = to_.begin[obs_node];
+    t.n_obs = (int32_t)to_.nvals(obs_node);
+    t.cols_off = cols_off;
+    t.n_cols = n_cols;
+    t.key = task_key(opts_.seed, f, stage, obs_node, src_node);
+    t.eps = st.eps;
+    int32_t est = st.n_est;
+    if (surrogate_) est = surrogate_rows(f, stage, obs_node, src_node, st.n_est);
+    t.rows0 = t.rows = std::min(std::max(est, opts_.min_samples), t.n_obs);
+    t.t_off = -1;
+    return t;
+  }
+  int32_t surrogate_rows(int32_t f, int32_t stage, int64_t o, int64_t s, int32_t fallback);
+
+  Context* ctx_;
+  const Tree& to_;
+  const Tree& ts_;
+  double k_, tol_;
+  bf_build_opts opts_;
+  Operator& op_;
+  cudaStream_t st_ = nullptr;
+  std::vector<BFState> bfs_;
+  std::unordered_map<KKey, SkelRef, KKeyHash> K_;
+  std::vector<int32_t> skel_;  // host skeleton pool (point ids)
+  // device
+  double* d_obs_ = nullptr;
+  double* d_src_ = nullptr;
+  int32_t* d_obs_perm_ = nullptr;
+  int32_t* d_colpool_ = nullptr;
+  int64_t colpool_cap_ = 0;
+  CTask* d_ctask_ = nullptr;
+  int64_t ctask_cap_ = 0;
+  float2* d_Z_ = nullptr;
+  int64_t z_cap_ = 0;
+  int32_t* d_rowpool_ = nullptr;
+  int64_t row_cap_ = 0;
+  int32_t* d_permpool_ = nullptr;
+  int64_t perm_cap_ = 0;
+  int32_t* d_skel_ = nullptr;
+  int64_t skel_cap_ = 0;
+  float2* d_raw_ = nullptr;
+  int64_t raw_cap_ = 0, raw_used_ = 0;
+  const Surrogate* surrogate_ = nullptr;
+  Surrogate sur_;
+  // stats
+  int64_t n_comp_ = 0, n_retry_ = 0, n_entries_ = 0;
+};
+
+int Builder::ensure_raw(int64_t need) {
+  if (need <= raw_cap_) return BF_OK;
+  int64_t n = std::max<int64_t>(need, raw_cap_ * 3 / 2);
+  n = std::max<int64_t>(n, 1 << 20);
+  float2* p = nullptr;
+  if (cudaMalloc(&p, (size_t)n * sizeof(float2)) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("build: cannot grow factor store to %lld entries", (long long)n);
+    return BF_ENOMEM;
+  }
+  if (d_raw_) {
+    BF_TRY_CUDA(cudaMemcpyAsync(p, d_raw_, (size_t)raw_used_ * sizeof(float2),
+                                cudaMemcpyDeviceToDevice, st_));
+    BF_TRY_CUDA(cudaStreamSynchronize(st_));
+    cudaFree(d_raw_);
+  }
+  d_raw_ = p;
+  raw_cap_ = n;
+  return BF_OK;
+}
+
+// PartialQR (compressors.jl:81-165) for a batch of compressions: sample,
+// pivoted QR, adaptive doubling of the sample while r > floor(0.8 rows), then
+// the interpolation matrix and the skeleton.
+int Builder::run_compressions(std::vector<HTask>& tasks, const std::vector<int32_t>& colpool) {
+  if (tasks.empty()) return BF_OK;
+  BF_TRY(dev_reserve(d_colpool_, colpool_cap_, (int64_t)colpool.size()));
+  BF_TRY_CUDA(cudaMemcpyAsync(d_colpool_, colpool.data(), colpool.size() * sizeof(int32_t),
+                              cudaMemcpyHostToDevice, st_));
+  // empty compressions (compressors.jl:93-96)
+  std::vector<int64_t> work;
+  for (int64_t i = 0; i < (int64_t)tasks.size(); ++i) {
+    HTask& t = tasks[i];
+    ++n_comp_;
+    if (t.n_obs == 0 || t.n_cols == 0) {
+      t.rank = 0;
+      t.t_off = raw_used_;
+      t.skel = SkelRef{(int64_t)skel_.size(), 0};
+      continue;
+    }
+    work.push_back(i);
+  }
+  const int64_t ZCAP = (int64_t)96 << 20;  // float2 entries per chunk (768 MB)
+  size_t pos = 0;
+  std::vector<CTask> ct;
+  std::vector<int64_t> pending, next, done;
+  std::vector<int32_t> hskel;
+  while (pos < work.size()) {
+    pending.clear();
+    int64_t zsum = 0;
+    while (pos < work.size()) {
+      const HTask& t = tasks[work[pos]];
+      int64_t z = (int64_t)t.rows * t.n_cols;
+      if (!pending.empty() && zsum + z > ZCAP) break;
+      zsum += z;
+      pending.push_back(work[pos++]);
+    }
+    while (!pending.empty()) {
+      // larger shared-memory needs last, so each QR launch covers one size bucket
+      std::stable_sort(pending.begin(), pending.end(), [&](int64_t a, int64_t b) {
+        return (int64_t)tasks[a].rows * tasks[a].n_cols < (int64_t)tasks[b].rows * tasks[b].n_cols;
+      });
+      int64_t np = (int64_t)pending.size();
+      ct.assign(np, CTask{});
+      int64_t zo = 0, ro = 0, po = 0;
+      for (int64_t q = 0; q < np; ++q) {
+        const HTask& t = tasks[pending[q]];
+        CTask& c = ct[q];
+        c.z_off = zo;
+        c.rows_off = ro;
+        c.cols_off = t.cols_off;
+        c.obs_begin = t.obs_begin;
+        c.perm_off = po;
+        c.t_off = -1;
+        c.skel_off = 0;
+        c.key = t.key;
+        c.eps = t.eps;
+        c.n_obs = t.n_obs;
+        c.n_rows = t.rows;
+        c.n_cols = t.n_cols;
+        c.rank = 0;
+        zo += (int64_t)t.rows * t.n_cols;
+        ro += t.rows;
+        po += t.n_cols;
+        n_entries_ += (int64_t)t.rows * t.n_cols;
+      }
+      BF_TRY(dev_reserve(d_ctask_, ctask_cap_, np));
+      BF_TRY(dev_reserve(d_Z_, z_cap_, zo));
+      BF_TRY(dev_reserve(d_rowpool_, row_cap_, ro));
+      BF_TRY(dev_reserve(d_permpool_, perm_cap_, po));
+      BF_TRY_CUDA(cudaMemcpyAsync(d_ctask_, ct.data(), np * sizeof(CTask), cudaMemcpyHostToDevice,
+                                  st_));
+      BF_TRY(launch_rows(d_ctask_, (int)np, d_obs_perm_, d_rowpool_, st_));
+      BF_TRY(launch_eval(d_ctask_, (int)np, d_obs_, d_src_, d_rowpool_, d_colpool_, d_Z_, k_, 0,
+                         st_));
+      // QR launches by shared-memory bucket
+      int64_t q0 = 0;
+      while (q0 < np) {
+        size_t need = qr_smem_bytes(ct[q0].n_rows, ct[q0].n_cols, true);
+        bool fits = need <= (size_t)QR_MAX_SMEM;
+        size_t cap = fits ? std::min<size_t>(QR_MAX_SMEM, std::max<size_t>(need * 2, 16384)) : 0;
+        int64_t q1 = q0;
+        size_t smax = 0;
+        while (q1 < np) {
+          size_t s = qr_smem_bytes(ct[q1].n_rows, ct[q1].n_cols, fits);
+          bool f1 = qr_smem_bytes(ct[q1].n_rows, ct[q1].n_cols, true) <= (size_t)QR_MAX_SMEM;
+          if (f1 != fits || (fits && s > cap)) break;
+          smax = std::max(smax, s);
+          ++q1;
+        }
+        if (!fits) smax = std::max(smax, qr_smem_bytes(0, 0, false));
+        BF_TRY(launch_qr(d_ctask_ + q0, (int)(q1 - q0), d_Z_, d_permpool_, fits, smax, st_));
+        q0 = q1;
+      }
+      BF_TRY_CUDA(cudaMemcpyAsync(ct.data(), d_ctask_, np * sizeof(CTask), cudaMemcpyDeviceToHost,
+                                  st_));
+      BF_TRY_CUDA(cudaStreamSynchronize(st_));
+      // adaptive decisions (compressors.jl:134-151)
+      next.clear();
+      done.clear();
+      int64_t tsum = 0, ssum = 0;
+      int max_rank = 0;
+      for (int64_t q = 0; q < np; ++q) {
+        HTask& t = tasks[pending[q]];
+        t.rank = ct[q].rank;
+        bool retry = opts_.adaptive && t.rank > (int32_t)std::floor(0.8 * t.rows) &&
+                     t.rows < t.n_obs;
+        if (retry) {
+          t.rows = std::min(t.rows * 2, t.n_obs);
+          t.retries++;
+          ++n_retry_;
+          next.push_back(pending[q]);
+        } else {
+          done.push_back(q);
+          tsum += (int64_t)t.rank * t.n_cols;
+          ssum += t.rank;
+          max_rank = std::max(max_rank, t.rank);
+        }
+      }
+      if (!done.empty()) {
+        BF_TRY(ensure_raw(raw_used_ + tsum));
+        BF_TRY(dev_reserve(d_skel_, skel_cap_, std::max<int64_t>(ssum, 1)));
+        std::vector<CTask> dct;
+        dct.reserve(done.size());
+        int64_t so = 0;
+        for (int64_t q : done) {
+          HTask& t = tasks[pending[q]];
+          CTask c = ct[q];
+          c.t_off = raw_used_;
+          c.skel_off = so;
+          t.t_off = raw_used_;
+          t.skel = SkelRef{(int64_t)skel_.size() + so, t.rank};
+          raw_used_ += (int64_t)t.rank * t.n_cols;
+          so += t.rank;
+          dct.push_back(c);
+        }
+        // done tasks reuse the front of the CTask buffer (their Z stays in place)
+        BF_TRY_CUDA(cudaMemcpyAsync(d_ctask_, dct.data(), dct.size() * sizeof(CTask),
+                                    cudaMemcpyHostToDevice, st_));
+        BF_TRY(launch_tsolve(d_ctask_, (int)dct.size(), d_Z_, d_permpool_, d_colpool_, d_raw_,
+                             d_skel_, max_rank, st_));
+        hskel.resize(ssum);
+        if (ssum > 0)
+          BF_TRY_CUDA(cudaMemcpyAsync(hskel.data(), d_skel_, ssum * sizeof(int32_t),
+                                      cudaMemcpyDeviceToHost, st_));
+        BF_TRY_CUDA(cudaStreamSynchronize(st_));
+        skel_.insert(skel_.end(), hskel.begin(), hskel.end());
+      }
+      pending.swap(next);
+    }
+  }
+  return BF_OK;
+}
+
+// Dense kernel blocks K(values(Oleaf), skeleton) for the P stage (bfassembly.jl:186-197).
+int Builder::run_dense(std::vector<HTask>& tasks, const std::vector<int32_t>& colpool) {
+  if (tasks.empty()) return BF_OK;
+  BF_TRY(dev_reserve(d_colpool_, colpool_cap_, (int64_t)colpool.size()));
+  BF_TRY_CUDA(cudaMemcpyAsync(d_colpool_, colpool.data(), colpool.size() * sizeof(int32_t),
+                              cudaMemcpyHostToDevice, st_));
+  int64_t tot = 0;
+  for (auto& t : tasks) tot += (int64_t)t.n_obs * t.n_cols;
+  BF_TRY(ensure_raw(raw_used_ + tot));
+  std::vector<CTask> ct(tasks.size());
+  for (size_t i = 0; i < tasks.size(); ++i) {
+    HTask& t = tasks[i];
+    CTask& c = ct[i];
+    c = CTask{};
+    c.rows_off = t.obs_begin;  // rows = values(Oleaf), a slice of the observer permutation
+    c.cols_off = t.cols_off;
+    c.n_rows = t.n_obs;
+    c.n_cols = t.n_cols;
+    c.t_off = raw_used_;
+    t.t_off = raw_used_;
+    raw_used_ += (int64_t)t.n_obs * t.n_cols;
+    n_entries_ += (int64_t)t.n_obs * t.n_cols;
+  }
+  const int64_t CH = 1 << 20;
+  for (int64_t b = 0; b < (int64_t)ct.size(); b += CH) {
+    int64_t n = std::min<int64_t>(CH, (int64_t)ct.size() - b);
+    BF_TRY(dev_reserve(d_ctask_, ctask_cap_, n));
+    BF_TRY_CUDA(cudaMemcpyAsync(d_ctask_, ct.data() + b, n * sizeof(CTask),
+                                cudaMemcpyHostToDevice, st_));
+    BF_TRY(launch_eval(d_ctask_, (int)n, d_obs_, d_src_, d_obs_perm_, d_colpool_, d_raw_, k_, 1,
+                       st_));
+    BF_TRY_CUDA(cudaStreamSynchronize(st_));
+  }
+  return BF_OK;
+}
+
+int32_t Builder::surrogate_rows(int32_t f, int32_t stage, int64_t o, int64_t s, int32_t fallback) {
+  const BFState& st = bfs_[f];
+  float feat[4];
+  surrogate_features(to_, ts_, k_, stage, o, s, feat);
+  float lr = sur_.predict_log_rank(feat);
+  int32_t r = (int32_t)std::ceil(std::exp((double)lr));
+  // sample enough rows that the predicted rank stays below the 0.8 retry line
+  int32_t rows = (int32_t)std::ceil(r / 0.8) + 2;
+  (void)st;
+  return std::max(rows, std::min(fallback, opts_.min_samples));
+}
+
+int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, int64_t n_src,
+                 const int64_t* far_obs, const int64_t* far_src, int64_t n_far) {
+  BF_TRY_CUDA(cudaSetDevice(ctx_->device));
+  if (!op_.stream) BF_TRY_CUDA(cudaStreamCreateWithFlags(&op_.stream, cudaStreamNonBlocking));
+  st_ = op_.stream;
+  if (opts_.rank_mode == 1) {
+    if (!opts_.surrogate_weights || !sur_.load(opts_.surrogate_weights, opts_.surrogate_nweights)) {
+      set_error("bf_build: rank_mode 1 needs valid surrogate weights");
+      return BF_EINVAL;
+    }
+    surrogate_ = &sur_;
+  }
+  // device copies of the geometry and of the observer permutation
+  BF_TRY_CUDA(cudaMalloc(&d_obs_, (size_t)n_obs * 3 * sizeof(double)));
+  BF_TRY_CUDA(cudaMalloc(&d_src_, (size_t)n_src * 3 * sizeof(double)));
+  BF_TRY_CUDA(cudaMemcpy(d_obs_, obs_xyz, n_obs * 3 * sizeof(double), cudaMemcpyHostToDevice));
+  BF_TRY_CUDA(cudaMemcpy(d_src_, src_xyz, n_src * 3 * sizeof(double), cudaMemcpyHostToDevice));
+  {
+    std::vector<int32_t> p(to_.perm.begin(), to_.perm.end());
+    BF_TRY_CUDA(cudaMalloc(&d_obs_perm_, p.size() * sizeof(int32_t)));
+    BF_TRY_CUDA(cudaMemcpy(d_obs_perm_, p.data(), p.size() * sizeof(int32_t),
+                           cudaMemcpyHostToDevice));
+  }
+  // per-far-pair state (bfassembly.jl:64-74)
+  bfs_.resize(n_far);
+  int32_t Lmax = 1;
+  for (int64_t f = 0; f < n_far; ++f) {
+    BFState& s = bfs_[f];
+    s.no = far_obs[f];
+    s.ns = far_src[f];
+    s.tS = traverse_and_pad(ts_, s.ns);
+    s.tO = traverse_and_pad(to_, s.no);
+    s.LS = (int32_t)s.tS.size();
+    s.LO = (int32_t)s.tO.size();
+    s.L = std::max(s.LS, s.LO);
+    s.eps = tol_ / s.L;
+    // ButterflyRankEstimator (rankestimation.jl:93-98), Rmin = 10
+    s.n_est = std::max((int32_t)std::ceil(opts_.c_tau * std::log(1.0 / s.eps)), 10);
+    Lmax = std::max(Lmax, s.L);
+  }
+  Logical& lg = op_.logical;
+  lg.n_rows = to_.n_points;
+  lg.n_cols = ts_.n_points;
+  lg.n_bf = (int32_t)n_far;
+  auto add_block = [&](int32_t bf, int32_t stage, int64_t oo, int64_t so, int64_t oi, int64_t si,
+                       int32_t rows, int32_t cols, int8_t ident, int64_t raw_off, int32_t ld) {
+    LBlock b;
+    b.bf = bf;
+    b.stage = stage;
+    b.oo = oo;
+    b.so = so;
+    b.oi = oi;
+    b.si = si;
+    b.rows = rows;
+    b.cols = cols;
+    b.ident = ident;
+    b.raw_off = raw_off;
+    b.raw_ld = std::max(ld, 1);
+    lg.blocks.push_back(b);
+  };
+  auto log_task = [&](const HTask& t) {
+    Operator::RankRec r;
+    r.bf = t.bf;
+    r.stage = t.stage;
+    r.obs_node = t.obs_node;
+    r.src_node = t.src_node;
+    r.n_obs = t.n_obs;
+    r.n_cols = t.n_cols;
+    r.rows0 = t.rows0;
+    r.rows = t.rows;
+    r.retries = t.retries;
+    r.rank = t.rank;
+    r.a_obs = (float)to_.radius(t.obs_node);
+    r.a_src = (float)ts_.radius(t.src_node);
+    double d2 = 0;
+    for (int a = 0; a < 3; ++a) {
+      double d = to_.center[3 * t.obs_node + a] - ts_.center[3 * t.src_node + a];
+      d2 += d * d;
+    }
+    r.dist = (float)std::sqrt(d2);
+    r.k = (float)k_;
+    op_.rank_log.push_back(r);
+  };
+
+  // ---- Q stage (bfassembly.jl:82-102)
+  {
+    std::vector<HTask> tasks;
+    std::vector<int32_t> pool;
+    for (int64_t f = 0; f < n_far; ++f) {
+      const BFState& s = bfs_[f];
+      for (int64_t Sleaf : s.tS.back()) {
+        int64_t off = (int64_t)pool.size();
+        add_values(pool, ts_, Sleaf);
+        tasks.push_back(make_task((int32_t)f, 0, s.no, Sleaf, off, (int32_t)ts_.nvals(Sleaf)));
+      }
+    }
+    BF_TRY(run_compressions(tasks, pool));
+    for (const HTask& t : tasks) {
+      add_block(t.bf, 0, t.obs_node, t.src_node, t.obs_node, t.src_node, t.rank, t.n_cols, 0,
+                t.t_off, t.rank);
+      K_[KKey{t.bf, t.src_node, t.obs_node}] = t.skel;
+      log_task(t);
+    }
+  }
+  // ---- R levels (bfassembly.jl:107-181)
+  for (int32_t l = 1; l < Lmax; ++l) {
+    std::vector<HTask> tasks;
+    std::vector<int32_t> pool;
+    std::vector<Item> items;
+    auto comp_item = [&](int32_t f, int64_t obs_node, int64_t svert, int64_t cols_off,
+                         int32_t ncols, int64_t oo, int64_t so, int64_t oi, int64_t si,
+                         int64_t split, int64_t us, int64_t uo) {
+      Item it{};
+      it.kind = 0;
+      it.bf = f;
+      it.oo = oo;
+      it.so = so;
+      it.oi = oi;
+      it.si = si;
+      it.split_svert = split;
+      it.upd_s = us;
+      it.upd_o = uo;
+      it.task = (int64_t)tasks.size();
+      tasks.push_back(make_task(f, l, obs_node, svert, cols_off, ncols));
+      items.push_back(it);
+    };
+    auto ident_item = [&](int32_t f, int64_t Overt, int64_t Svert) {
+      Item it{};
+      it.kind = 1;
+      it.bf = f;
+      it.oo = it.oi = Overt;
+      it.so = it.si = Svert;
+      it.split_svert = -1;
+      it.upd_s = Svert;
+      it.upd_o = Overt;
+      it.task = -1;
+      it.copy = K_.at(KKey{f, Svert, Overt});
+      items.push_back(it);
+    };
+    // U(Svert, Overt): concatenated child skeletons (bfassembly.jl:206-230)
+    auto push_U = [&](int32_t f, int64_t Svert, int64_t Overt, int64_t& off, int32_t& len) {
+      off = (int64_t)pool.size();
+      if (!ts_.isleaf(Svert)) {
+        for (int32_t c = 0; c < ts_.n_child[Svert]; ++c)
+          add_skel(pool, K_.at(KKey{f, ts_.first_child[Svert] + c, Overt}));
+      } else {
+        add_skel(pool, K_.at(KKey{f, Svert, Overt}));
+      }
+      len = (int32_t)((int64_t)pool.size() - off);
+    };
+    for (int64_t f = 0; f < n_far; ++f) {
+      const BFState& s = bfs_[f];
+      if (l >= s.L) continue;
+      const int32_t fi = (int32_t)f;
+      bool sfz = l >= s.LS, ofz = l >= s.LO;
+      if (!sfz && !ofz) {  // build_nonfrozen_R_blocks (bfassembly.jl:232-349)
+        const auto& olv = s.tO[l - 1];
+        const auto& slv = s.tS[s.LS - l - 1];
+        for (int64_t Svert : slv)
+          for (int64_t Overt : olv) {
+            bool sleaf = ts_.isleaf(Svert);
+            if (!to_.isleaf(Overt)) {
+              int64_t off;
+              int32_t len;
+              push_U(fi, Svert, Overt, off, len);
+              for (int32_t c = 0; c < to_.n_child[Overt]; ++c) {
+                int64_t Oc = to_.first_child[Overt] + c;
+                comp_item(fi, Oc, Svert, off, len, Oc, Svert, Overt, Svert, sleaf ? -1 : Svert,
+                          Svert, Oc);
+              }
+            } else if (!sleaf) {
+              int64_t off;
+              int32_t len;
+              push_U(fi, Svert, Overt, off, len);
+              comp_item(fi, Overt, Svert, off, len, Overt, Svert, Overt, Svert, Svert, Svert,
+                        Overt);
+            } else {
+              ident_item(fi, Overt, Svert);
+            }
+          }
+      } else if (sfz && !ofz) {  // build_sourcefrozen_R_blocks (bfassembly.jl:351-412)
+        int64_t Svert = s.ns;
+        for (int64_t Overt : s.tO[l - 1]) {
+          if (!to_.isleaf(Overt)) {
+            SkelRef ref = K_.at(KKey{fi, Svert, Overt});
+            int64_t off = (int64_t)pool.size();
+            add_skel(pool, ref);
+            for (int32_t c = 0; c < to_.n_child[Overt]; ++c) {
+              int64_t Oc = to_.first_child[Overt] + c;
+              comp_item(fi, Oc, Svert, off, ref.len, Oc, Svert, Overt, Svert, -1, Svert, Oc);
+            }
+          } else {
+            ident_item(fi, Overt, Svert);
+          }
+        }
+      } else {  // build_observerfrozen_R_blocks (bfassembly.jl:414-481)
+        const auto& olv = s.tO[s.LO - 1];
+        const auto& slv = s.tS[s.LS - l - 1];
+        for (int64_t Svert : slv)
+          for (int64_t Overt : olv) {
+            if (!ts_.isleaf(Svert)) {
+              int64_t off;
+              int32_t len;
+              push_U(fi, Svert, Overt, off, len);
+              comp_item(fi, Overt, Svert, off, len, Overt, Svert, Overt, Svert, Svert, Svert,
+                        Overt);
+            } else {
+              ident_item(fi, Overt, Svert);
+            }
+          }
+      }
+    }
+    BF_TRY(run_compressions(tasks, pool));
+    // emit blocks, then apply the skeleton updates (deferred as in bfassembly.jl:177-180)
+    std::vector<std::pair<KKey, SkelRef>> upd;
+    upd.reserve(items.size());
+    for (const Item& it : items) {
+      if (it.kind == 1) {
+        add_block(it.bf, l, it.oo, it.so, it.oi, it.si, 0, 0, 1, 0, 1);
+        upd.push_back({KKey{it.bf, it.upd_s, it.upd_o}, it.copy});
+        continue;
+      }
+      const HTask& t = tasks[it.task];
+      if (it.split_svert < 0) {
+        add_block(it.bf, l, it.oo, it.so, it.oi, it.si, t.rank, t.n_cols, 0, t.t_off, t.rank);
+      } else {
+        int64_t c0 = 0;
+        int64_t Sv = it.split_svert;
+        for (int32_t c = 0; c < ts_.n_child[Sv]; ++c) {
+          int64_t Sc = ts_.first_child[Sv] + c;
+          int32_t ks = K_.at(KKey{it.bf, Sc, it.oi}).len;
+          add_block(it.bf, l, it.oo, it.so, it.oi, Sc, t.rank, ks, 0, t.t_off + c0 * t.rank,
+                    t.rank);
+          c0 += ks;
+        }
+      }
+      upd.push_back({KKey{it.bf, it.upd_s, it.upd_o}, t.skel});
+    }
+    for (const HTask& t : tasks) log_task(t);
+    for (auto& u : upd) K_[u.first] = u.second;
+  }
+  // ---- P stage (bfassembly.jl:186-197)
+  {
+    std::vector<HTask> tasks;
+    std::vector<int32_t> pool;
+    for (int64_t f = 0; f < n_far; ++f) {
+      const BFState& s = bfs_[f];
+      for (int64_t Oleaf : s.tO.back()) {
+        SkelRef ref = K_.at(KKey{(int32_t)f, s.ns, Oleaf});
+        HTask t{};
+        t.bf = (int32_t)f;
+        t.obs_node = Oleaf;
+        t.src_node = s.ns;
+        t.obs_begin = to_.begin[Oleaf];
+        t.n_obs = (int32_t)to_.nvals(Oleaf);
+        t.cols_off = (int64_t)pool.size();
+        t.n_cols = ref.len;
+        add_skel(pool, ref);
+        tasks.push_back(t);
+      }
+    }
+    BF_TRY(run_dense(tasks, pool));
+    for (const HTask& t : tasks)
+      add_block(t.bf, -1, t.obs_node, t.src_node, t.obs_node, t.src_node, t.n_obs, t.n_cols, 0,
+                t.t_off, t.n_obs);
+  }
+  // node -> values maps for the packer
+  auto fill_vm = [](ValuesMap& vm, const Tree& t) {
+    vm.ptr.assign(t.nn() + 1, 0);
+    for (int64_t i = 0; i < t.nn(); ++i) vm.ptr[i + 1] = vm.ptr[i] + t.nvals(i);
+    vm.idx.resize(vm.ptr[t.nn()]);
+    for (int64_t i = 0; i < t.nn(); ++i)
+      std::memcpy(vm.idx.data() + vm.ptr[i], t.vals(i), t.nvals(i) * sizeof(int64_t));
+  };
+  fill_vm(lg.obs_vals, to_);
+  fill_vm(lg.src_vals, ts_);
+  op_.raw_is_double = 0;
+  op_.d_raw = d_raw_;
+  op_.raw_entries = raw_used_;
+  d_raw_ = nullptr;
+  op_.stats.compressions = n_comp_;
+  op_.stats.retries = n_retry_;
+  op_.stats.kernel_entries = n_entries_;
+  return BF_OK;
+}
+
+}  // namespace
+
+int build_operator(Context* ctx, const double* obs_xyz, int64_t n_obs, const double* src_xyz,
+                   int64_t n_src, const Tree& to, const Tree& ts, const int64_t* far_obs,
+                   const int64_t* far_src, int64_t n_far, double k, double tol,
+                   const bf_build_opts& opts, Operator& op) {
+  auto t0 = std::chrono::steady_clock::now();
+  op.ctx = ctx;
+  {
+    Builder b(ctx, to, ts, k, tol, opts, op);
+    BF_TRY(b.run(obs_xyz, n_obs, src_xyz, n_src, far_obs, far_src, n_far));
+  }
+  BF_TRY(pack_plan(op.logical, op.plan));
+  BF_TRY(upload_plan(op));
+  BF_TRY_CUDA(cudaDeviceSynchronize());
+  auto t1 = std::chrono::steady_clock::now();
+  op.stats.build_seconds = std::chrono::duration<double>(t1 - t0).count();
+  return BF_OK;
+}
+
+}  // namespace bfg
+
+using namespace bfg;
+
+extern "C" int bf_build(bf_ctx_t ctx, const double* obs_xyz, int64_t n_obs,
+                        const double* src_xyz, int64_t n_src, bf_tree_t obs_tree,
+                        bf_tree_t src_tree, const int64_t* far_obs, const int64_t* far_src,
+                        int64_t n_far, double k, double tol, const bf_build_opts* opts,
+                        bf_op_t* out) {
+  try {
+    if (!out) {
+      set_error("bf_build: out is NULL");
+      return BF_EINVAL;
+    }
+    *out = nullptr;
+    if (!ctx || !obs_xyz || !src_xyz || !obs_tree || !src_tree || !far_obs || !far_src ||
+        n_far <= 0 || !(k > 0) || !(tol > 0)) {
+      set_error("bf_build: invalid argument");
+      return BF_EINVAL;
+    }
+    if (obs_tree->t.n_points != n_obs || src_tree->t.n_points != n_src) {
+      set_error("bf_build: tree point counts do not match the geometry");
+      return BF_EINVAL;
+    }
+    if (n_obs >= ((int64_t)1 << 31) || n_src >= ((int64_t)1 << 31)) {
+      set_error("bf_build: point sets above 2^31 are not supported");
+      return BF_ENOTSUP;
+    }
+    for (int64_t f = 0; f < n_far; ++f)
+      if (far_obs[f] < 0 || far_obs[f] >= obs_tree->t.nn() || far_src[f] < 0 ||
+          far_src[f] >= src_tree->t.nn()) {
+        set_error("bf_build: far pair %lld references an unknown node", (long long)f);
+        return BF_EINVAL;
+      }
+    bf_build_opts o;
+    if (opts)
+      o = *opts;
+    else
+      bf_build_opts_default(&o);
+    if (o.min_samples < 1) o.min_samples = 1;
+    auto* h = new bf_operator;
+    int s = build_operator(&ctx->c, obs_xyz, n_obs, src_xyz, n_src, obs_tree->t, src_tree->t,
+                           far_obs, far_src, n_far, k, tol, o, h->op);
+    if (s != BF_OK) {
+      delete h;
+      return s;
+    }
+    *out = h;
+    return BF_OK;
+  } catch (const std::bad_alloc&) {
+    set_error("bf_build: host allocation failed");
+    return BF_ENOMEM;
+  } catch (const std::out_of_range&) {
+    set_error("bf_build: internal skeleton lookup failed");
+    return BF_EINVAL;
+  } catch (...) {
+    set_error("bf_build: unexpected internal error");
+    return BF_EINVAL;
+  }
+}

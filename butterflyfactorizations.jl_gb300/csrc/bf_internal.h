@@ -107,6 +107,7 @@ struct Plan {
   int64_t ws_entries = 0;
   std::vector<DTask> tasks;
   std::vector<int64_t> stage_begin;  // n_stages + 1
+  std::vector<int64_t> stage_bytes;  // algorithmic bytes of each level launch
   std::vector<int32_t> maps;
   int64_t a_entries = 0;
   std::vector<DSeg> segs;
@@ -146,12 +147,37 @@ struct Operator {
   // mixed path
   void* mixed = nullptr;
   bf_op_stats stats{};
+  // per-compression rank records of the build (surrogate training data)
+  struct RankRec {
+    int32_t bf, stage;
+    int64_t obs_node, src_node;
+    int32_t n_obs, n_cols, rows0, rows, retries, rank;
+    float a_obs, a_src, dist, k;
+  };
+  std::vector<RankRec> rank_log;
   ~Operator();
 };
 
 int upload_plan(Operator& op);  // repacks d_raw into d_A, uploads tasks/maps, allocates ws
+int build_operator(Context* ctx, const double* obs_xyz, int64_t n_obs, const double* src_xyz,
+                   int64_t n_src, const Tree& to, const Tree& ts, const int64_t* far_obs,
+                   const int64_t* far_src, int64_t n_far, double k, double tol,
+                   const bf_build_opts& opts, Operator& op);
+int profile_matvec(Operator& op, int trans, int nrep, double* ms, int64_t* bytes,
+                   int64_t* kernels);
 int run_matvec(Operator& op, int trans, int64_t nrhs, const double* x, int64_t ldx, double* y,
                int64_t ldy, const double* alpha, const double* beta, int ptr_mode,
                cudaStream_t stream);
 
 }  // namespace bfg
+
+// opaque C-ABI handles
+struct bf_tree {
+  bfg::Tree t;
+};
+struct bf_context {
+  bfg::Context c;
+};
+struct bf_operator {
+  bfg::Operator op;
+};

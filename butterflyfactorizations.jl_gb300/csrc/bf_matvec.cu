@@ -320,6 +320,54 @@ static int matvec_one(Operator& op, int trans, const double2* x, double2* y, dou
   return BF_OK;
 }
 
+// Per-stage device time of one matvec: events around every level launch.
+int profile_matvec(Operator& op, int trans, int nrep, double* ms, int64_t* bytes,
+                   int64_t* kernels) {
+  const Plan& p = op.plan;
+  const int64_t ns = p.n_stages();
+  if (nrep < 1) nrep = 1;
+  BF_TRY_CUDA(cudaSetDevice(op.ctx->device));
+  cudaStream_t st = op.stream;
+  std::vector<cudaEvent_t> ev(ns + 1);
+  for (auto& e : ev) BF_TRY_CUDA(cudaEventCreate(&e));
+  std::vector<double> acc(ns, 0.0);
+  const bool fwd = trans == BF_OP_N;
+  for (int r = 0; r < nrep + 1; ++r) {  // first pass warms up
+    BF_TRY_CUDA(cudaEventRecord(ev[0], st));
+    for (int64_t k = 0; k < ns; ++k) {
+      int64_t s = fwd ? k : ns - 1 - k;
+      int64_t b = p.stage_begin[s], e = p.stage_begin[s + 1];
+      if (e > b) {
+        const DTask* tk = op.d_tasks + b;
+        if (fwd)
+          stage_fwd_kernel<<<(unsigned)(e - b), NT, 0, st>>>(tk, op.d_A, op.d_maps, op.d_ws);
+        else if (trans == BF_OP_C)
+          stage_adj_kernel<true><<<(unsigned)(e - b), NT, 0, st>>>(tk, op.d_A, op.d_maps, op.d_ws);
+        else
+          stage_adj_kernel<false><<<(unsigned)(e - b), NT, 0, st>>>(tk, op.d_A, op.d_maps, op.d_ws);
+      }
+      BF_TRY_CUDA(cudaEventRecord(ev[k + 1], st));
+    }
+    BF_TRY_CUDA(cudaEventSynchronize(ev[ns]));
+    if (r == 0) continue;
+    for (int64_t k = 0; k < ns; ++k) {
+      float t = 0.f;
+      BF_TRY_CUDA(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
+      int64_t s = fwd ? k : ns - 1 - k;
+      acc[s] += t;
+    }
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  int64_t nk = 2;  // split + combine
+  for (int64_t s = 0; s < ns; ++s) {
+    if (ms) ms[s] = acc[s] / nrep;
+    if (bytes) bytes[s] = p.stage_bytes[s];
+    if (p.stage_begin[s + 1] > p.stage_begin[s]) ++nk;
+  }
+  if (kernels) *kernels = nk;
+  return BF_OK;
+}
+
 int run_matvec(Operator& op, int trans, int64_t nrhs, const double* x, int64_t ldx, double* y,
                int64_t ldy, const double* alpha, const double* beta, int ptr_mode,
                cudaStream_t stream) {

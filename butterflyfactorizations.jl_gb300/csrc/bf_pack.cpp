@@ -330,7 +330,9 @@ int pack_plan(const Logical& lg, Plan& plan) {
   int64_t a_off = 0;
   int64_t alg = 0;
   for (int32_t s = 0; s <= Lmax; ++s) {
+    int64_t sbytes = 0;
     for (auto& t : stages[s]) {
+      sbytes += 16 * (t.M + t.n);
       if (t.M > INT32_MAX || t.n > INT32_MAX) {
         set_error("pack: task too large");
         return BF_ENOTSUP;
@@ -387,6 +389,7 @@ int pack_plan(const Logical& lg, Plan& plan) {
             g.rows = k.rows;
             g.cols = k.cols;
             plan.block_entries += (int64_t)k.rows * k.cols;
+            sbytes += 16 * (int64_t)k.rows * k.cols;
             plan.max_rank = std::max<int64_t>(plan.max_rank, k.rows);
           }
           if (g.rows > 0 && g.cols > 0) plan.segs.push_back(g);
@@ -398,6 +401,7 @@ int pack_plan(const Logical& lg, Plan& plan) {
       plan.tasks.push_back(d);
     }
     plan.stage_begin.push_back((int64_t)plan.tasks.size());
+    plan.stage_bytes.push_back(sbytes);
   }
   plan.a_entries = a_off;
   plan.yg_covered = std::all_of(ycov.begin(), ycov.end(), [](uint8_t c) { return c != 0; });

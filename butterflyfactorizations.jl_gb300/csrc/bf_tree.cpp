@@ -148,9 +148,6 @@ bool is_far(const Tree& ts, const Tree& to, int64_t snode, int64_t onode, double
 
 using namespace bfg;
 
-struct bf_tree {
-  Tree t;
-};
 
 extern "C" {
 

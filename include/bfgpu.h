@@ -209,12 +209,31 @@ typedef struct {
 
 BF_API int bf_op_stats_get(bf_op_t op, bf_op_stats* stats);
 
-/* Copy back the factors as the reference block list (same layout as
- * bf_factor_desc).  Call with data == NULL to query n_blocks and n_data. */
-BF_API int bf_op_export_blocks(bf_op_t op, int64_t* n_blocks, int64_t* n_data, int32_t* bf,
-                               int32_t* stage, int64_t* obs_out, int64_t* src_out,
-                               int64_t* obs_in, int64_t* src_in, int32_t* rows, int32_t* cols,
-                               int8_t* identity, int64_t* data_off, double* data);
+/* Copy back the factors of far blocks bf_begin <= bf < bf_end as the
+ * reference block list (same layout as bf_factor_desc; data_off counts complex
+ * entries from the first exported block).  Call with data == NULL to query
+ * n_blocks and n_data.  as_float32 != 0 writes complex64 (pairs of float) into
+ * data, which is exact for factors built by bf_build. */
+BF_API int bf_op_export_blocks(bf_op_t op, int64_t bf_begin, int64_t bf_end, int64_t* n_blocks,
+                               int64_t* n_data, int32_t* bf, int32_t* stage, int64_t* obs_out,
+                               int64_t* src_out, int64_t* obs_in, int64_t* src_in,
+                               int32_t* rows, int32_t* cols, int8_t* identity, int64_t* data_off,
+                               void* data, int32_t as_float32);
+
+/* Rank records of the build, one per compression (the richer form of the
+ * reference RankLogger, src/ButterflyFactorization/bfstructs.jl:220-232 and
+ * compressors.jl:153): 14 values per record in rec[14*i ...]:
+ * bf, stage, obs_node, src_node, n_obs, n_cols, rows_initial, rows_final,
+ * retries, rank, radius_obs, radius_src, center_distance, k.
+ * Call with rec == NULL to query *n_rec. */
+BF_API int bf_op_rank_log(bf_op_t op, int64_t* n_rec, double* rec);
+
+/* Device time of each level launch of one matvec (CUDA events on the handle's
+ * stream, mean over nrep passes) and the algorithmic bytes each launch moves
+ * (factor entries + vector entries read and written, 16 B per complex
+ * entry).  Arrays have n_stages entries (bf_op_stats.n_stages). */
+BF_API int bf_op_profile(bf_op_t op, int trans, int32_t nrep, double* ms_per_stage,
+                         int64_t* bytes_per_stage, int64_t* kernels_per_matvec);
 
 BF_API int bf_op_destroy(bf_op_t op);
 

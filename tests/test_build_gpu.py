@@ -1,0 +1,101 @@
+"""GPU construction (bf_build): accuracy against dense products and parity of
+the GPU matvec with the reference-order CPU matvec on the GPU-built factors.
+
+Construction parity is statistical (the reference samples rows with an
+unseeded RNG, compressors.jl:101); the acceptance criteria are the reference
+tests' ``< 10*tol`` against dense products (test/test_subroutines.jl:174-182,
+test/test_pgalerkin.jl:155-156).  The library samples the same rows as the
+oracle for the same seed, so structure (compression count, ranks) is compared
+too.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import bfgpu
+from bfgpu import geometry as G
+from oracle import bfref as O
+from _util import export_to_oracle, relerr
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def c1(ctx):
+    obs, src = G.plane_pair(4096, seed=1)
+    k = 2 * math.pi / 0.125
+    to, ts = bfgpu.Tree.build(obs, max_depth=4), bfgpu.Tree.build(src, max_depth=4)
+    op = bfgpu.assemble_BF(obs, src, to, ts, 0, 0, k, TOL, c_tau=4.0, seed=3, ctx=ctx)
+    kern = O.HelmholtzKernel(obs, src, k)
+    return dict(obs=obs, src=src, k=k, to=to, ts=ts, op=op, kern=kern)
+
+
+def test_c1_build_matches_dense(c1):
+    A = c1["kern"](np.arange(4096), np.arange(4096))
+    x = G.complex_gaussian(4096, 7)
+    assert relerr(c1["op"] @ x, A @ x) < 10 * TOL
+    assert relerr(c1["op"].adjoint() @ x, A.conj().T @ x) < 10 * TOL
+    st = c1["op"].stats()
+    assert st["compressions"] == 1280
+    assert st["build_seconds"] > 0
+
+
+def test_c1_build_structure_matches_oracle(c1):
+    ot = O.build_tree(c1["obs"], max_depth=4)
+    os_ = O.build_tree(c1["src"], max_depth=4)
+    bf = O.assemble_bf(c1["kern"], ot, os_, 0, 0, c1["k"], TOL, c_tau=4.0, seed=3)
+    ex = c1["op"].export_blocks()
+    gbf = export_to_oracle(ex, ot, os_)[0]
+    assert len(gbf.Q) == len(bf.Q) and len(gbf.P) == len(bf.P)
+    assert [len(l) for l in gbf.R] == [len(l) for l in bf.R]
+    # same sampled rows; FP32 vs FP64 QR may differ in the last rank only
+    rq = np.array([b.data.shape[0] for b in gbf.Q])
+    ro = np.array([b.data.shape[0] for b in bf.Q])
+    assert np.mean(np.abs(rq - ro) <= 1) > 0.95
+
+
+def test_matvec_parity_on_gpu_built_factors(c1):
+    ot = O.build_tree(c1["obs"], max_depth=4)
+    os_ = O.build_tree(c1["src"], max_depth=4)
+    gbf = export_to_oracle(c1["op"].export_blocks(), ot, os_)[0]
+    x = G.complex_gaussian(4096, 8)
+    ref = O.matvec_flat(gbf, x, np.zeros(4096, complex))
+    assert relerr(c1["op"] @ x, ref) <= 1e-12
+    refa = O.matvec_flat(O.adjoint_bf(gbf), x, np.zeros(4096, complex))
+    assert relerr(c1["op"].adjoint() @ x, refa) <= 1e-12
+
+
+@pytest.mark.parametrize("deep_obs", [True, False])
+def test_unbalanced_build_matches_dense(ctx, deep_obs):
+    obs, src = G.plane_pair(1500, seed=4, z_obs=2.5)
+    k = 2 * math.pi / 0.25
+    to = bfgpu.Tree.build(obs, max_points=12 if deep_obs else 200)
+    ts = bfgpu.Tree.build(src, max_points=200 if deep_obs else 12)
+    op = bfgpu.assemble_BF(obs, src, to, ts, 0, 0, k, TOL, seed=1, ctx=ctx)
+    A = O.HelmholtzKernel(obs, src, k)(np.arange(1500), np.arange(1500))
+    x = G.complex_gaussian(1500, 1)
+    assert relerr(op @ x, A @ x) < 10 * TOL
+    assert relerr(op.adjoint() @ x, A.conj().T @ x) < 10 * TOL
+
+
+def test_far_operator_build_matches_dense(ctx):
+    n = 4000
+    pts = G.fibonacci_sphere(n)
+    k = G.wavenumber(n, 4 * math.pi)
+    t = bfgpu.Tree.build(pts, max_points=24)
+    op = bfgpu.PetrovGalerkinBF(pts, pts, t, t, k, tol=TOL, ctx=ctx)
+    ot = O.build_tree(pts, max_points=24)
+    far, _ = O.nearandfar(ot, ot, 1.0)
+    kern = O.HelmholtzKernel(pts, pts, k)
+    D = O.dense_far(kern, O.FarOperator([O.BF([], [], [], ot, ot, k, TOL, o, s)
+                                         for o, s in far], far, n, n))
+    x = G.complex_gaussian(n, 2)
+    assert relerr(op @ x, D @ x) < 10 * TOL
+    assert relerr(op.adjoint() @ x, D.conj().T @ x) < 10 * TOL
+    assert op.stats()["n_bf"] == len(far)
+    # parity on the built factors against the reference-order far-field driver
+    bfs = export_to_oracle(op.export_blocks(), ot, ot)
+    fop = O.FarOperator(bfs, far, n, n)
+    assert relerr(op @ x, O.far_matvec(fop, x)) <= 1e-12

@@ -173,3 +173,20 @@ def test_oracle_reproduces_golden_fixtures(name):
         assert np.array_equal(d[key], g[key]), key
     assert relerr(d["data"], g["data"]) < 1e-12
     assert relerr(O.far_matvec(far, g["x"]), g["y"]) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["plane_single", "plane_unbalanced", "sphere_far"])
+def test_c_restatement_matches_golden(name):
+    import os
+    from oracle.cbind import CRefOperator
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", f"{name}.npz"))
+    blocks = {k: g[k] for k in ["bf", "stage", "obs_out", "src_out", "obs_in", "src_in", "rows",
+                                "cols", "identity", "data_off", "data"]}
+    op = CRefOperator(int(g["n_rows"]), int(g["n_cols"]), blocks, (g["obs_ptr"], g["obs_idx"]),
+                      (g["src_ptr"], g["src_idx"]))
+    for nt in (1, 4):
+        assert relerr(op.matvec(g["x"], nthreads=nt), g["y"]) < 1e-13
+    y0 = G.complex_gaussian(int(g["n_rows"]), 5)
+    y = y0.copy()
+    op.matvec(g["x"], y, alpha=0.5 + 1j, beta=-2.0, nthreads=2)
+    assert relerr(y, -2.0 * y0 + (0.5 + 1j) * g["y"]) < 1e-13
