@@ -234,7 +234,10 @@ def run_ours(args, rank, world, local):
     op = w["op"]
     n = w["n"]
     st = op.stats()
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the legacy default stream has handle 0, which the C ABI
+    # reads as "use the operator's own stream"
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sp = stream.cuda_stream
     xd = torch.from_numpy(w["x"]).to(f"cuda:{local}")
     yd = torch.zeros_like(xd)

@@ -108,6 +108,11 @@ struct Plan {
   std::vector<DTask> tasks;
   std::vector<int64_t> stage_begin;  // n_stages + 1
   std::vector<int64_t> stage_bytes;  // algorithmic bytes of each level launch
+  // forward launch lists per stage: warp items (task, first row) and wide tasks
+  std::vector<int32_t> fw_items;        // flattened (task, row0) pairs
+  std::vector<int64_t> fw_items_begin;  // n_stages + 1, in pairs
+  std::vector<int32_t> wide_tasks;      // tasks with M <= 32 and n > 2M
+  std::vector<int64_t> wide_begin;      // n_stages + 1
   std::vector<int32_t> maps;
   int64_t a_entries = 0;
   std::vector<DSeg> segs;
@@ -140,6 +145,8 @@ struct Operator {
   DTask* d_tasks = nullptr;
   int32_t* d_maps = nullptr;
   float4* d_ws = nullptr;
+  int32_t* d_items = nullptr;  // forward warp items (pairs)
+  int32_t* d_wide = nullptr;   // forward wide tasks
   // staging of host right-hand sides
   double* d_x = nullptr;
   double* d_y = nullptr;

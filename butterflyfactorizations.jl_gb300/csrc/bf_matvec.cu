@@ -218,6 +218,129 @@ __global__ void combine_kernel(double2* __restrict__ y, int64_t n, const float4*
   }
 }
 
+// ---------------------------------------------------------------------------
+// Forward, warp per 32-row panel.  Lanes own rows; each column of the
+// column-major task matrix is one coalesced 512-byte warp load (LDG.128 per
+// lane); the input entries of a column block sit in warp-private shared memory
+// and are read as broadcasts.  Tasks with M <= 16 use G = 32/M lane groups
+// that walk interleaved columns, so one warp load still covers G*M contiguous
+// entries; the groups are summed at the end.  No block-level barrier.
+constexpr int FW_WARPS = 8;
+constexpr int FW_XB = 256;
+
+__global__ void __launch_bounds__(FW_WARPS * 32) fwd_rows_kernel(
+    const int2* __restrict__ items, int n_items, const DTask* __restrict__ tasks,
+    const float4* __restrict__ A, const int32_t* __restrict__ maps, float4* __restrict__ ws) {
+  __shared__ float4 xs[FW_WARPS][FW_XB];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int item = blockIdx.x * FW_WARPS + warp;
+  if (item >= n_items) return;
+  const int2 it = items[item];
+  const DTask t = tasks[it.x];
+  const int32_t* __restrict__ rmap = maps + t.rmap_off;
+  const int32_t* __restrict__ cmap = maps + t.cmap_off;
+  const int M = t.M, n = t.n, r0 = it.y;
+  if (t.kind == TASK_COPY) {
+    const int i = r0 + lane;
+    if (i < M) ws[rmap[i]] = ws[cmap[i]];
+    return;
+  }
+  int G = 1, g = 0, i = r0 + lane;
+  if (M <= 16) {
+    G = 32 / M;
+    g = lane / M;
+    i = lane - g * M;
+  }
+  const bool active = g < G && i < M;
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  float4* __restrict__ xw = xs[warp];
+  for (int cb = 0; cb < n; cb += FW_XB) {
+    const int nb = min(FW_XB, n - cb);
+    for (int j = lane; j < nb; j += 32) xw[j] = ws[cmap[cb + j]];
+    __syncwarp();
+    if (active) {
+      const size_t step = (size_t)G * M;
+      const float4* __restrict__ ap = A + t.a_off + (size_t)(cb + g) * M + i;
+      int j = g;
+      for (; j + 3 * G < nb; j += 4 * G) {  // four independent loads in flight
+        const float4 a0 = __ldg(ap), a1 = __ldg(ap + step), a2 = __ldg(ap + 2 * step),
+                     a3 = __ldg(ap + 3 * step);
+        cdf_mac(acc, a0, xw[j]);
+        cdf_mac(acc, a1, xw[j + G]);
+        cdf_mac(acc, a2, xw[j + 2 * G]);
+        cdf_mac(acc, a3, xw[j + 3 * G]);
+        ap += 4 * step;
+      }
+      for (; j < nb; j += G) {
+        cdf_mac(acc, __ldg(ap), xw[j]);
+        ap += step;
+      }
+    }
+    __syncwarp();
+  }
+  if (G > 1) {
+    xw[lane] = acc;  // reuse the warp's staging buffer for the group reduction
+    __syncwarp();
+    if (active && g == 0) {
+      for (int q = 1; q < G; ++q) cdf_add(acc, xw[q * M + i]);
+      ws[rmap[i]] = cdf_norm(acc);
+    }
+  } else if (active) {
+    ws[rmap[i]] = cdf_norm(acc);
+  }
+}
+
+// Forward for short wide tasks (M <= 32, many columns: the P stage).  One CTA
+// per task; warps split the columns, lane groups (G = 32/M per warp) read G*M
+// contiguous entries per load; partial row sums meet in shared memory.
+__global__ void __launch_bounds__(256) fwd_wide_kernel(const int32_t* __restrict__ tlist,
+                                                       const DTask* __restrict__ tasks,
+                                                       const float4* __restrict__ A,
+                                                       const int32_t* __restrict__ maps,
+                                                       float4* __restrict__ ws) {
+  __shared__ float4 red[8][32];
+  const DTask t = tasks[tlist[blockIdx.x]];
+  const int32_t* __restrict__ rmap = maps + t.rmap_off;
+  const int32_t* __restrict__ cmap = maps + t.cmap_off;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int M = t.M, n = t.n;
+  const int G = 32 / M;
+  const int g = lane / M, i = lane - g * M;
+  const bool active = g < G;
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (active) {
+    const int cstep = 8 * G;
+    const size_t step = (size_t)cstep * M;
+    int j = warp * G + g;
+    const float4* __restrict__ ap = A + t.a_off + (size_t)j * M + i;
+    for (; j + 3 * cstep < n; j += 4 * cstep) {
+      const float4 a0 = __ldg(ap), a1 = __ldg(ap + step), a2 = __ldg(ap + 2 * step),
+                   a3 = __ldg(ap + 3 * step);
+      const float4 x0 = ws[cmap[j]], x1 = ws[cmap[j + cstep]], x2 = ws[cmap[j + 2 * cstep]],
+                   x3 = ws[cmap[j + 3 * cstep]];
+      cdf_mac(acc, a0, x0);
+      cdf_mac(acc, a1, x1);
+      cdf_mac(acc, a2, x2);
+      cdf_mac(acc, a3, x3);
+      ap += 4 * step;
+    }
+    for (; j < n; j += cstep) {
+      cdf_mac(acc, __ldg(ap), ws[cmap[j]]);
+      ap += step;
+    }
+  }
+  red[warp][lane] = acc;
+  __syncthreads();
+  if (threadIdx.x < M) {
+    const int r = threadIdx.x;
+    float4 v = red[0][r];
+    for (int q = 1; q < G; ++q) cdf_add(v, red[0][q * M + r]);
+    for (int w = 1; w < 8; ++w)
+      for (int q = 0; q < G; ++q) cdf_add(v, red[w][q * M + r]);
+    ws[rmap[r]] = cdf_norm(v);
+  }
+}
+
 inline int grid_for(int64_t n, int threads) {
   int64_t g = (n + threads - 1) / threads;
   return (int)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 16));
@@ -231,6 +354,8 @@ Operator::~Operator() {
   if (d_tasks) cudaFree(d_tasks);
   if (d_maps) cudaFree(d_maps);
   if (d_ws) cudaFree(d_ws);
+  if (d_items) cudaFree(d_items);
+  if (d_wide) cudaFree(d_wide);
   if (d_x) cudaFree(d_x);
   if (d_y) cudaFree(d_y);
   if (stream) cudaStreamDestroy(stream);
@@ -276,6 +401,14 @@ int upload_plan(Operator& op) {
     return BF_ENOMEM;
   }
   BF_TRY_CUDA(cudaMemset(op.d_ws, 0, (size_t)std::max<int64_t>(p.ws_entries, 1) * sizeof(float4)));
+  BF_TRY_CUDA(cudaMalloc(&op.d_items, std::max<size_t>(1, p.fw_items.size()) * sizeof(int32_t)));
+  if (!p.fw_items.empty())
+    BF_TRY_CUDA(cudaMemcpy(op.d_items, p.fw_items.data(), p.fw_items.size() * sizeof(int32_t),
+                           cudaMemcpyHostToDevice));
+  BF_TRY_CUDA(cudaMalloc(&op.d_wide, std::max<size_t>(1, p.wide_tasks.size()) * sizeof(int32_t)));
+  if (!p.wide_tasks.empty())
+    BF_TRY_CUDA(cudaMemcpy(op.d_wide, p.wide_tasks.data(), p.wide_tasks.size() * sizeof(int32_t),
+                           cudaMemcpyHostToDevice));
   op.stats.n_bf = p.n_bf;
   op.stats.n_stages = p.n_stages();
   op.stats.n_tasks = (int64_t)p.tasks.size();
@@ -286,6 +419,36 @@ int upload_plan(Operator& op) {
   op.stats.alg_bytes_fwd = p.alg_bytes_fwd;
   op.stats.max_rank = p.max_rank;
   return BF_OK;
+}
+
+// Launches of level s for direction trans; returns the number of kernels.
+static int launch_stage(Operator& op, int64_t s, int trans, cudaStream_t st) {
+  const Plan& p = op.plan;
+  int nk = 0;
+  if (trans == BF_OP_N) {
+    int64_t ib = p.fw_items_begin[s], ie = p.fw_items_begin[s + 1];
+    if (ie > ib) {
+      unsigned blocks = (unsigned)((ie - ib + FW_WARPS - 1) / FW_WARPS);
+      fwd_rows_kernel<<<blocks, FW_WARPS * 32, 0, st>>>(
+          (const int2*)op.d_items + ib, (int)(ie - ib), op.d_tasks, op.d_A, op.d_maps, op.d_ws);
+      ++nk;
+    }
+    int64_t wb = p.wide_begin[s], we = p.wide_begin[s + 1];
+    if (we > wb) {
+      fwd_wide_kernel<<<(unsigned)(we - wb), 256, 0, st>>>(op.d_wide + wb, op.d_tasks, op.d_A,
+                                                           op.d_maps, op.d_ws);
+      ++nk;
+    }
+    return nk;
+  }
+  int64_t b = p.stage_begin[s], e = p.stage_begin[s + 1];
+  if (e <= b) return 0;
+  const DTask* tk = op.d_tasks + b;
+  if (trans == BF_OP_C)
+    stage_adj_kernel<true><<<(unsigned)(e - b), NT, 0, st>>>(tk, op.d_A, op.d_maps, op.d_ws);
+  else
+    stage_adj_kernel<false><<<(unsigned)(e - b), NT, 0, st>>>(tk, op.d_A, op.d_maps, op.d_ws);
+  return 1;
 }
 
 // One FP64-accurate matvec of a single right-hand side, device pointers.
@@ -302,18 +465,7 @@ static int matvec_one(Operator& op, int trans, const double2* x, double2* y, dou
   if (!covered)
     BF_TRY_CUDA(cudaMemsetAsync(op.d_ws + out_off, 0, (size_t)nout * sizeof(float4), st));
   const int64_t ns = p.n_stages();
-  for (int64_t k = 0; k < ns; ++k) {
-    int64_t s = fwd ? k : ns - 1 - k;
-    int64_t b = p.stage_begin[s], e = p.stage_begin[s + 1];
-    if (e <= b) continue;
-    const DTask* tk = op.d_tasks + b;
-    if (fwd)
-      stage_fwd_kernel<<<(unsigned)(e - b), NT, 0, st>>>(tk, op.d_A, op.d_maps, op.d_ws);
-    else if (trans == BF_OP_C)
-      stage_adj_kernel<true><<<(unsigned)(e - b), NT, 0, st>>>(tk, op.d_A, op.d_maps, op.d_ws);
-    else
-      stage_adj_kernel<false><<<(unsigned)(e - b), NT, 0, st>>>(tk, op.d_A, op.d_maps, op.d_ws);
-  }
+  for (int64_t k = 0; k < ns; ++k) launch_stage(op, fwd ? k : ns - 1 - k, trans, st);
   combine_kernel<<<grid_for(nout, 256), 256, 0, st>>>(y, nout, op.d_ws, out_off, alpha, beta,
                                                       beta.x == 0.0 && beta.y == 0.0, 0);
   BF_TRY_CUDA(cudaGetLastError());
@@ -332,22 +484,16 @@ int profile_matvec(Operator& op, int trans, int nrep, double* ms, int64_t* bytes
   for (auto& e : ev) BF_TRY_CUDA(cudaEventCreate(&e));
   std::vector<double> acc(ns, 0.0);
   const bool fwd = trans == BF_OP_N;
+  int64_t nk = 2;  // split + combine
   for (int r = 0; r < nrep + 1; ++r) {  // first pass warms up
     BF_TRY_CUDA(cudaEventRecord(ev[0], st));
+    int64_t cnt = 2;
     for (int64_t k = 0; k < ns; ++k) {
-      int64_t s = fwd ? k : ns - 1 - k;
-      int64_t b = p.stage_begin[s], e = p.stage_begin[s + 1];
-      if (e > b) {
-        const DTask* tk = op.d_tasks + b;
-        if (fwd)
-          stage_fwd_kernel<<<(unsigned)(e - b), NT, 0, st>>>(tk, op.d_A, op.d_maps, op.d_ws);
-        else if (trans == BF_OP_C)
-          stage_adj_kernel<true><<<(unsigned)(e - b), NT, 0, st>>>(tk, op.d_A, op.d_maps, op.d_ws);
-        else
-          stage_adj_kernel<false><<<(unsigned)(e - b), NT, 0, st>>>(tk, op.d_A, op.d_maps, op.d_ws);
-      }
+      cnt += launch_stage(op, fwd ? k : ns - 1 - k, trans, st);
       BF_TRY_CUDA(cudaEventRecord(ev[k + 1], st));
     }
+    BF_TRY_CUDA(cudaGetLastError());
+    nk = cnt;
     BF_TRY_CUDA(cudaEventSynchronize(ev[ns]));
     if (r == 0) continue;
     for (int64_t k = 0; k < ns; ++k) {
@@ -358,11 +504,9 @@ int profile_matvec(Operator& op, int trans, int nrep, double* ms, int64_t* bytes
     }
   }
   for (auto& e : ev) cudaEventDestroy(e);
-  int64_t nk = 2;  // split + combine
   for (int64_t s = 0; s < ns; ++s) {
     if (ms) ms[s] = acc[s] / nrep;
     if (bytes) bytes[s] = p.stage_bytes[s];
-    if (p.stage_begin[s + 1] > p.stage_begin[s]) ++nk;
   }
   if (kernels) *kernels = nk;
   return BF_OK;

@@ -404,6 +404,29 @@ int pack_plan(const Logical& lg, Plan& plan) {
     plan.stage_bytes.push_back(sbytes);
   }
   plan.a_entries = a_off;
+  // forward launch lists: short wide tasks get a CTA each, the rest one warp
+  // per 32-row panel (a single warp item when M <= 16)
+  plan.fw_items_begin.push_back(0);
+  plan.wide_begin.push_back(0);
+  for (int64_t s = 0; s + 1 < (int64_t)plan.stage_begin.size(); ++s) {
+    for (int64_t gi = plan.stage_begin[s]; gi < plan.stage_begin[s + 1]; ++gi) {
+      const DTask& d = plan.tasks[gi];
+      if (d.M <= 0) continue;
+      if (d.kind == TASK_DENSE && d.M <= 32 && d.n > 2 * d.M) {
+        plan.wide_tasks.push_back((int32_t)gi);
+      } else if (d.kind == TASK_DENSE && d.M <= 16) {
+        plan.fw_items.push_back((int32_t)gi);
+        plan.fw_items.push_back(0);
+      } else {
+        for (int32_t r0 = 0; r0 < d.M; r0 += 32) {
+          plan.fw_items.push_back((int32_t)gi);
+          plan.fw_items.push_back(r0);
+        }
+      }
+    }
+    plan.fw_items_begin.push_back((int64_t)plan.fw_items.size() / 2);
+    plan.wide_begin.push_back((int64_t)plan.wide_tasks.size());
+  }
   plan.yg_covered = std::all_of(ycov.begin(), ycov.end(), [](uint8_t c) { return c != 0; });
   plan.xg_covered = std::all_of(xcov.begin(), xcov.end(), [](uint8_t c) { return c != 0; });
   int64_t slot_total = 0;
