@@ -252,6 +252,9 @@ def run_ours(args, rank, world, local):
     torch.cuda.synchronize()
     clk = ClockSampler(local)
     clk.start()
+    for _ in range(2):  # bring clocks back up after the sampler's start-up pause
+        step()
+    torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)

@@ -276,6 +276,16 @@ class Operator:
         check(lib.bf_op_rank_log(self._h, C.byref(n), _p(rec, C.c_double)), "rank_log")
         return rec[:n.value]
 
+    def task_shapes(self):
+        """(stage, kind, M, n) int32 arrays of the packed level tasks."""
+        lib = load()
+        n = C.c_int64()
+        check(lib.bf_op_task_shapes(self._h, C.byref(n), None, None, None, None), "task_shapes")
+        a = [np.zeros(max(n.value, 1), np.int32) for _ in range(4)]
+        check(lib.bf_op_task_shapes(self._h, C.byref(n), *[_p(v, C.c_int32) for v in a]),
+              "task_shapes")
+        return tuple(v[:n.value] for v in a)
+
     def profile(self, nrep: int = 5):
         """Per-level launch times (ms), algorithmic bytes and kernels per matvec."""
         lib = load()

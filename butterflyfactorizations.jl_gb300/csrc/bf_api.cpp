@@ -370,6 +370,29 @@ int bf_op_profile(bf_op_t h, int trans, int32_t nrep, double* ms_per_stage,
   BF_GUARD_END
 }
 
+int bf_op_task_shapes(bf_op_t h, int64_t* n_tasks, int32_t* stage, int32_t* kind, int32_t* M,
+                      int32_t* n) {
+  if (!h || !n_tasks) {
+    set_error("bf_op_task_shapes: NULL argument");
+    return BF_EINVAL;
+  }
+  const Plan& p = h->op.plan;
+  *n_tasks = (int64_t)p.tasks.size();
+  if (!stage) return BF_OK;
+  if (!kind || !M || !n) {
+    set_error("bf_op_task_shapes: NULL output array");
+    return BF_EINVAL;
+  }
+  for (int64_t s = 0; s < p.n_stages(); ++s)
+    for (int64_t t = p.stage_begin[s]; t < p.stage_begin[s + 1]; ++t) {
+      stage[t] = (int32_t)s;
+      kind[t] = p.tasks[t].kind;
+      M[t] = p.tasks[t].M;
+      n[t] = p.tasks[t].n;
+    }
+  return BF_OK;
+}
+
 int bf_op_destroy(bf_op_t op) {
   if (op) {
     cudaSetDevice(op->op.ctx->device);

@@ -81,6 +81,11 @@ struct Logical {
 // ---------------------------------------------------------------- packed plan
 enum : int32_t { TASK_DENSE = 0, TASK_COPY = 1 };
 
+// task shape classes of the forward kernels
+constexpr int TALL_ROWS = 128;  // rows per tall-kernel warp item
+constexpr int FLAT_MMAX = 128;  // flat kernel: 32 < M <= FLAT_MMAX
+constexpr int FLAT_NMAX = 256;  //              n <= FLAT_NMAX
+
 // Device task descriptor: row side = rmap[0..M), column side = cmap[0..n);
 // forward computes ws[rmap] = A * ws[cmap]; adjoint ws[cmap] = A^H * ws[rmap].
 struct alignas(16) DTask {
@@ -108,11 +113,12 @@ struct Plan {
   std::vector<DTask> tasks;
   std::vector<int64_t> stage_begin;  // n_stages + 1
   std::vector<int64_t> stage_bytes;  // algorithmic bytes of each level launch
-  // forward launch lists per stage: warp items (task, first row) and wide tasks
-  std::vector<int32_t> fw_items;        // flattened (task, row0) pairs
-  std::vector<int64_t> fw_items_begin;  // n_stages + 1, in pairs
-  std::vector<int32_t> wide_tasks;      // tasks with M <= 32 and n > 2M
-  std::vector<int64_t> wide_begin;      // n_stages + 1
+  // forward launch lists (one per task shape class, see bf_matvec.cu), all
+  // concatenated in `lists`; begin[c][s] indexes class c at stage s (in
+  // entries; tall items are (task, row0) pairs and count two entries each)
+  enum { L_TALL = 0, L_FLAT, L_SMALL, L_WIDE, L_COPY, L_NCLASS };
+  std::vector<int32_t> lists;
+  std::vector<int64_t> list_begin[L_NCLASS];  // n_stages + 1 each
   std::vector<int32_t> maps;
   int64_t a_entries = 0;
   std::vector<DSeg> segs;
@@ -145,8 +151,7 @@ struct Operator {
   DTask* d_tasks = nullptr;
   int32_t* d_maps = nullptr;
   float4* d_ws = nullptr;
-  int32_t* d_items = nullptr;  // forward warp items (pairs)
-  int32_t* d_wide = nullptr;   // forward wide tasks
+  int32_t* d_lists = nullptr;  // forward launch lists (Plan::lists)
   // staging of host right-hand sides
   double* d_x = nullptr;
   double* d_y = nullptr;

@@ -219,16 +219,20 @@ __global__ void combine_kernel(double2* __restrict__ y, int64_t n, const float4*
 }
 
 // ---------------------------------------------------------------------------
-// Forward, warp per 32-row panel.  Lanes own rows; each column of the
-// column-major task matrix is one coalesced 512-byte warp load (LDG.128 per
-// lane); the input entries of a column block sit in warp-private shared memory
-// and are read as broadcasts.  Tasks with M <= 16 use G = 32/M lane groups
-// that walk interleaved columns, so one warp load still covers G*M contiguous
-// entries; the groups are summed at the end.  No block-level barrier.
+// Forward kernels, chosen per task shape by the packer (bf_pack.cpp):
+//   tall  (M > 128): warp per 128-row panel, 4 rows per lane;
+//   flat  (32 < M <= 128, n <= 256): warp per task streaming all M*n entries;
+//   small (M <= 32): warp per task, G = 32/M lane groups on interleaved columns;
+//   wide  (M <= 32, n > 2M): CTA per task (fwd_wide_kernel);
+//   copy  (identity blocks): warp per task.
+// All of them read every factor entry exactly once with coalesced 128-bit
+// loads straight from HBM; input entries are gathered once per warp into
+// shared memory and read as broadcasts.  No block-level barriers.
 constexpr int FW_WARPS = 8;
-constexpr int FW_XB = 256;
+constexpr int FW_XB = 256;  // staged input entries per warp per pass
+constexpr int TALL_RPL = TALL_ROWS / 32;  // rows per lane in the tall kernel
 
-__global__ void __launch_bounds__(FW_WARPS * 32) fwd_rows_kernel(
+__global__ void __launch_bounds__(FW_WARPS * 32) fwd_tall_kernel(
     const int2* __restrict__ items, int n_items, const DTask* __restrict__ tasks,
     const float4* __restrict__ A, const int32_t* __restrict__ maps, float4* __restrict__ ws) {
   __shared__ float4 xs[FW_WARPS][FW_XB];
@@ -240,18 +244,118 @@ __global__ void __launch_bounds__(FW_WARPS * 32) fwd_rows_kernel(
   const int32_t* __restrict__ rmap = maps + t.rmap_off;
   const int32_t* __restrict__ cmap = maps + t.cmap_off;
   const int M = t.M, n = t.n, r0 = it.y;
-  if (t.kind == TASK_COPY) {
-    const int i = r0 + lane;
-    if (i < M) ws[rmap[i]] = ws[cmap[i]];
-    return;
+  float4 acc[TALL_RPL];
+#pragma unroll
+  for (int q = 0; q < TALL_RPL; ++q) acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+  bool act[TALL_RPL];
+#pragma unroll
+  for (int q = 0; q < TALL_RPL; ++q) act[q] = r0 + lane + 32 * q < M;
+  float4* __restrict__ xw = xs[warp];
+  for (int cb = 0; cb < n; cb += FW_XB) {
+    const int nb = min(FW_XB, n - cb);
+    for (int j = lane; j < nb; j += 32) xw[j] = ws[cmap[cb + j]];
+    __syncwarp();
+    const float4* __restrict__ ap = A + t.a_off + (size_t)cb * M + r0 + lane;
+    int j = 0;
+    for (; j + 1 < nb; j += 2) {  // 2 columns x 4 rows: eight loads in flight
+      float4 a[2][TALL_RPL];
+#pragma unroll
+      for (int c = 0; c < 2; ++c)
+#pragma unroll
+        for (int q = 0; q < TALL_RPL; ++q)
+          a[c][q] = act[q] ? __ldg(ap + (size_t)c * M + 32 * q) : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float4 x0 = xw[j], x1 = xw[j + 1];
+#pragma unroll
+      for (int q = 0; q < TALL_RPL; ++q) {
+        cdf_mac(acc[q], a[0][q], x0);
+        cdf_mac(acc[q], a[1][q], x1);
+      }
+      ap += 2 * (size_t)M;
+    }
+    if (j < nb) {
+      const float4 x0 = xw[j];
+#pragma unroll
+      for (int q = 0; q < TALL_RPL; ++q)
+        if (act[q]) cdf_mac(acc[q], __ldg(ap + 32 * q), x0);
+    }
+    __syncwarp();
   }
-  int G = 1, g = 0, i = r0 + lane;
-  if (M <= 16) {
-    G = 32 / M;
-    g = lane / M;
-    i = lane - g * M;
+#pragma unroll
+  for (int q = 0; q < TALL_RPL; ++q)
+    if (act[q]) ws[rmap[r0 + lane + 32 * q]] = cdf_norm(acc[q]);
+}
+
+// One warp streams a whole task flat: lane l reads entry e = l + 32k of the
+// column-major M x n matrix.  With M > 32 the 32 entries of one warp load
+// belong to 32 distinct rows, so each lane adds its product into a per-row
+// accumulator in warp-private shared memory without conflicts.
+__global__ void __launch_bounds__(FW_WARPS * 32) fwd_flat_kernel(
+    const int32_t* __restrict__ tlist, int n_tasks, const DTask* __restrict__ tasks,
+    const float4* __restrict__ A, const int32_t* __restrict__ maps, float4* __restrict__ ws) {
+  __shared__ float4 xs[FW_WARPS][FLAT_NMAX];
+  __shared__ float4 as[FW_WARPS][FLAT_MMAX];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ti = blockIdx.x * FW_WARPS + warp;
+  if (ti >= n_tasks) return;
+  const DTask t = tasks[tlist[ti]];
+  const int32_t* __restrict__ rmap = maps + t.rmap_off;
+  const int32_t* __restrict__ cmap = maps + t.cmap_off;
+  const int M = t.M, n = t.n;
+  float4* __restrict__ xw = xs[warp];
+  float4* __restrict__ aw = as[warp];
+  for (int j = lane; j < n; j += 32) xw[j] = ws[cmap[j]];
+  for (int i = lane; i < M; i += 32) aw[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  __syncwarp();
+  const long long tot = (long long)M * n;
+  const float4* __restrict__ ap = A + t.a_off;
+  int row = lane, col = 0;  // entry lane: row lane of column 0 (M > 32)
+  long long e = lane;
+  for (; e + 96 < tot; e += 128) {  // four loads in flight
+    const float4 a0 = __ldg(ap + e), a1 = __ldg(ap + e + 32), a2 = __ldg(ap + e + 64),
+                 a3 = __ldg(ap + e + 96);
+    const float4 v[4] = {a0, a1, a2, a3};
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      float4 s = aw[row];
+      cdf_mac(s, v[u], xw[col]);
+      aw[row] = s;
+      row += 32;
+      if (row >= M) {
+        row -= M;
+        ++col;
+      }
+    }
   }
-  const bool active = g < G && i < M;
+  for (; e < tot; e += 32) {
+    float4 s = aw[row];
+    cdf_mac(s, __ldg(ap + e), xw[col]);
+    aw[row] = s;
+    row += 32;
+    if (row >= M) {
+      row -= M;
+      ++col;
+    }
+  }
+  __syncwarp();
+  for (int i = lane; i < M; i += 32) ws[rmap[i]] = cdf_norm(aw[i]);
+}
+
+// M <= 32: G = 32/M lane groups walk interleaved columns (one warp load reads
+// G*M contiguous entries); the groups meet in shared memory at the end.
+__global__ void __launch_bounds__(FW_WARPS * 32) fwd_small_kernel(
+    const int32_t* __restrict__ tlist, int n_tasks, const DTask* __restrict__ tasks,
+    const float4* __restrict__ A, const int32_t* __restrict__ maps, float4* __restrict__ ws) {
+  __shared__ float4 xs[FW_WARPS][FW_XB];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ti = blockIdx.x * FW_WARPS + warp;
+  if (ti >= n_tasks) return;
+  const DTask t = tasks[tlist[ti]];
+  const int32_t* __restrict__ rmap = maps + t.rmap_off;
+  const int32_t* __restrict__ cmap = maps + t.cmap_off;
+  const int M = t.M, n = t.n;
+  const int G = 32 / M;
+  const int g = lane / M, i = lane - g * M;
+  const bool active = g < G;
   float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
   float4* __restrict__ xw = xs[warp];
   for (int cb = 0; cb < n; cb += FW_XB) {
@@ -262,7 +366,7 @@ __global__ void __launch_bounds__(FW_WARPS * 32) fwd_rows_kernel(
       const size_t step = (size_t)G * M;
       const float4* __restrict__ ap = A + t.a_off + (size_t)(cb + g) * M + i;
       int j = g;
-      for (; j + 3 * G < nb; j += 4 * G) {  // four independent loads in flight
+      for (; j + 3 * G < nb; j += 4 * G) {
         const float4 a0 = __ldg(ap), a1 = __ldg(ap + step), a2 = __ldg(ap + 2 * step),
                      a3 = __ldg(ap + 3 * step);
         cdf_mac(acc, a0, xw[j]);
@@ -279,7 +383,7 @@ __global__ void __launch_bounds__(FW_WARPS * 32) fwd_rows_kernel(
     __syncwarp();
   }
   if (G > 1) {
-    xw[lane] = acc;  // reuse the warp's staging buffer for the group reduction
+    xw[lane] = acc;  // reuse the staging buffer for the group reduction
     __syncwarp();
     if (active && g == 0) {
       for (int q = 1; q < G; ++q) cdf_add(acc, xw[q * M + i]);
@@ -287,6 +391,24 @@ __global__ void __launch_bounds__(FW_WARPS * 32) fwd_rows_kernel(
     }
   } else if (active) {
     ws[rmap[i]] = cdf_norm(acc);
+  }
+}
+
+// identity blocks: copy the input slot to the output slot
+__global__ void copy_kernel(const int32_t* __restrict__ tlist, int n_tasks,
+                            const DTask* __restrict__ tasks, const int32_t* __restrict__ maps,
+                            float4* __restrict__ ws, int reverse) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ti = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (ti >= n_tasks) return;
+  const DTask t = tasks[tlist[ti]];
+  const int32_t* __restrict__ rmap = maps + t.rmap_off;
+  const int32_t* __restrict__ cmap = maps + t.cmap_off;
+  for (int i = lane; i < t.M; i += 32) {
+    if (reverse)
+      ws[cmap[i]] = ws[rmap[i]];
+    else
+      ws[rmap[i]] = ws[cmap[i]];
   }
 }
 
@@ -354,8 +476,7 @@ Operator::~Operator() {
   if (d_tasks) cudaFree(d_tasks);
   if (d_maps) cudaFree(d_maps);
   if (d_ws) cudaFree(d_ws);
-  if (d_items) cudaFree(d_items);
-  if (d_wide) cudaFree(d_wide);
+  if (d_lists) cudaFree(d_lists);
   if (d_x) cudaFree(d_x);
   if (d_y) cudaFree(d_y);
   if (stream) cudaStreamDestroy(stream);
@@ -401,13 +522,9 @@ int upload_plan(Operator& op) {
     return BF_ENOMEM;
   }
   BF_TRY_CUDA(cudaMemset(op.d_ws, 0, (size_t)std::max<int64_t>(p.ws_entries, 1) * sizeof(float4)));
-  BF_TRY_CUDA(cudaMalloc(&op.d_items, std::max<size_t>(1, p.fw_items.size()) * sizeof(int32_t)));
-  if (!p.fw_items.empty())
-    BF_TRY_CUDA(cudaMemcpy(op.d_items, p.fw_items.data(), p.fw_items.size() * sizeof(int32_t),
-                           cudaMemcpyHostToDevice));
-  BF_TRY_CUDA(cudaMalloc(&op.d_wide, std::max<size_t>(1, p.wide_tasks.size()) * sizeof(int32_t)));
-  if (!p.wide_tasks.empty())
-    BF_TRY_CUDA(cudaMemcpy(op.d_wide, p.wide_tasks.data(), p.wide_tasks.size() * sizeof(int32_t),
+  BF_TRY_CUDA(cudaMalloc(&op.d_lists, std::max<size_t>(1, p.lists.size()) * sizeof(int32_t)));
+  if (!p.lists.empty())
+    BF_TRY_CUDA(cudaMemcpy(op.d_lists, p.lists.data(), p.lists.size() * sizeof(int32_t),
                            cudaMemcpyHostToDevice));
   op.stats.n_bf = p.n_bf;
   op.stats.n_stages = p.n_stages();
@@ -426,17 +543,41 @@ static int launch_stage(Operator& op, int64_t s, int trans, cudaStream_t st) {
   const Plan& p = op.plan;
   int nk = 0;
   if (trans == BF_OP_N) {
-    int64_t ib = p.fw_items_begin[s], ie = p.fw_items_begin[s + 1];
-    if (ie > ib) {
-      unsigned blocks = (unsigned)((ie - ib + FW_WARPS - 1) / FW_WARPS);
-      fwd_rows_kernel<<<blocks, FW_WARPS * 32, 0, st>>>(
-          (const int2*)op.d_items + ib, (int)(ie - ib), op.d_tasks, op.d_A, op.d_maps, op.d_ws);
+    auto range = [&](int c, int64_t& b, int64_t& n) {
+      b = p.list_begin[c][s];
+      n = p.list_begin[c][s + 1] - b;
+    };
+    int64_t b, n;
+    const unsigned WT = FW_WARPS * 32;
+    range(Plan::L_TALL, b, n);
+    if (n > 0) {
+      int64_t items = n / 2;
+      fwd_tall_kernel<<<(unsigned)((items + FW_WARPS - 1) / FW_WARPS), WT, 0, st>>>(
+          (const int2*)(op.d_lists + b), (int)items, op.d_tasks, op.d_A, op.d_maps, op.d_ws);
       ++nk;
     }
-    int64_t wb = p.wide_begin[s], we = p.wide_begin[s + 1];
-    if (we > wb) {
-      fwd_wide_kernel<<<(unsigned)(we - wb), 256, 0, st>>>(op.d_wide + wb, op.d_tasks, op.d_A,
-                                                           op.d_maps, op.d_ws);
+    range(Plan::L_FLAT, b, n);
+    if (n > 0) {
+      fwd_flat_kernel<<<(unsigned)((n + FW_WARPS - 1) / FW_WARPS), WT, 0, st>>>(
+          op.d_lists + b, (int)n, op.d_tasks, op.d_A, op.d_maps, op.d_ws);
+      ++nk;
+    }
+    range(Plan::L_SMALL, b, n);
+    if (n > 0) {
+      fwd_small_kernel<<<(unsigned)((n + FW_WARPS - 1) / FW_WARPS), WT, 0, st>>>(
+          op.d_lists + b, (int)n, op.d_tasks, op.d_A, op.d_maps, op.d_ws);
+      ++nk;
+    }
+    range(Plan::L_WIDE, b, n);
+    if (n > 0) {
+      fwd_wide_kernel<<<(unsigned)n, 256, 0, st>>>(op.d_lists + b, op.d_tasks, op.d_A,
+                                                   op.d_maps, op.d_ws);
+      ++nk;
+    }
+    range(Plan::L_COPY, b, n);
+    if (n > 0) {
+      copy_kernel<<<(unsigned)((n + 7) / 8), 256, 0, st>>>(op.d_lists + b, (int)n, op.d_tasks,
+                                                           op.d_maps, op.d_ws, 0);
       ++nk;
     }
     return nk;

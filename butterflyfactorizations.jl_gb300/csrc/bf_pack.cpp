@@ -404,28 +404,39 @@ int pack_plan(const Logical& lg, Plan& plan) {
     plan.stage_bytes.push_back(sbytes);
   }
   plan.a_entries = a_off;
-  // forward launch lists: short wide tasks get a CTA each, the rest one warp
-  // per 32-row panel (a single warp item when M <= 16)
-  plan.fw_items_begin.push_back(0);
-  plan.wide_begin.push_back(0);
-  for (int64_t s = 0; s + 1 < (int64_t)plan.stage_begin.size(); ++s) {
-    for (int64_t gi = plan.stage_begin[s]; gi < plan.stage_begin[s + 1]; ++gi) {
-      const DTask& d = plan.tasks[gi];
-      if (d.M <= 0) continue;
-      if (d.kind == TASK_DENSE && d.M <= 32 && d.n > 2 * d.M) {
-        plan.wide_tasks.push_back((int32_t)gi);
-      } else if (d.kind == TASK_DENSE && d.M <= 16) {
-        plan.fw_items.push_back((int32_t)gi);
-        plan.fw_items.push_back(0);
-      } else {
-        for (int32_t r0 = 0; r0 < d.M; r0 += 32) {
-          plan.fw_items.push_back((int32_t)gi);
-          plan.fw_items.push_back(r0);
+  // forward launch lists by task shape (kernels in bf_matvec.cu)
+  {
+    std::vector<int32_t> cls[Plan::L_NCLASS];
+    for (auto& b : plan.list_begin) b.assign(1, 0);
+    std::vector<std::vector<int64_t>> ends(Plan::L_NCLASS);
+    for (int64_t s = 0; s + 1 < (int64_t)plan.stage_begin.size(); ++s) {
+      for (int64_t gi = plan.stage_begin[s]; gi < plan.stage_begin[s + 1]; ++gi) {
+        const DTask& d = plan.tasks[gi];
+        if (d.M <= 0) continue;
+        if (d.kind == TASK_COPY) {
+          cls[Plan::L_COPY].push_back((int32_t)gi);
+        } else if (d.M <= 32 && d.n > 2 * d.M) {
+          cls[Plan::L_WIDE].push_back((int32_t)gi);
+        } else if (d.M <= 32) {
+          cls[Plan::L_SMALL].push_back((int32_t)gi);
+        } else if (d.M <= FLAT_MMAX && d.n <= FLAT_NMAX) {
+          cls[Plan::L_FLAT].push_back((int32_t)gi);
+        } else {
+          for (int32_t r0 = 0; r0 < d.M; r0 += TALL_ROWS) {
+            cls[Plan::L_TALL].push_back((int32_t)gi);
+            cls[Plan::L_TALL].push_back(r0);
+          }
         }
       }
+      for (int c = 0; c < Plan::L_NCLASS; ++c) ends[c].push_back((int64_t)cls[c].size());
     }
-    plan.fw_items_begin.push_back((int64_t)plan.fw_items.size() / 2);
-    plan.wide_begin.push_back((int64_t)plan.wide_tasks.size());
+    // concatenate; list_begin holds absolute offsets into plan.lists
+    for (int c = 0; c < Plan::L_NCLASS; ++c) {
+      int64_t base = (int64_t)plan.lists.size();
+      plan.list_begin[c].assign(1, base);
+      for (int64_t e : ends[c]) plan.list_begin[c].push_back(base + e);
+      plan.lists.insert(plan.lists.end(), cls[c].begin(), cls[c].end());
+    }
   }
   plan.yg_covered = std::all_of(ycov.begin(), ycov.end(), [](uint8_t c) { return c != 0; });
   plan.xg_covered = std::all_of(xcov.begin(), xcov.end(), [](uint8_t c) { return c != 0; });

@@ -235,6 +235,12 @@ BF_API int bf_op_rank_log(bf_op_t op, int64_t* n_rec, double* rec);
 BF_API int bf_op_profile(bf_op_t op, int trans, int32_t nrep, double* ms_per_stage,
                          int64_t* bytes_per_stage, int64_t* kernels_per_matvec);
 
+/* Shapes of the packed level tasks (stage index, kind 0 = dense / 1 = copy,
+ * rows M, columns n), in launch order.  Call with stage == NULL to query
+ * *n_tasks.  Used by the tile autotuner and by diagnostics. */
+BF_API int bf_op_task_shapes(bf_op_t op, int64_t* n_tasks, int32_t* stage, int32_t* kind,
+                             int32_t* M, int32_t* n);
+
 BF_API int bf_op_destroy(bf_op_t op);
 
 #ifdef __cplusplus
