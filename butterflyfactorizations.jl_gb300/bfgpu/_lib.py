@@ -60,6 +60,7 @@ SIGNATURES = [
     ("bf_matvec", C.c_int, [vp, C.c_int, i64, vp, i64, vp, i64, P(f64), P(f64), C.c_int, vp]),
     ("bf_matvec_mixed", C.c_int, [vp, C.c_int, i64, vp, i64, vp, i64, P(f64), P(f64), C.c_int,
                                   vp]),
+    ("bf_matvec_noalloc", C.c_int, [vp, C.c_int, i64, vp, i64, vp, i64, P(f64), P(f64), vp]),
     ("bf_op_size", C.c_int, [vp, P(i64), P(i64)]),
     ("bf_op_stats_get", C.c_int, [vp, P(OpStats)]),
     ("bf_op_export_blocks", C.c_int, [vp, i64, i64, P(i64), P(i64), P(i32), P(i32), P(i64),

@@ -12,6 +12,7 @@
 // products run on the FP32 pipes at ~1e-14 relative accuracy; GB300's FP64
 // rate (about 1.2 TFLOP/s) cannot feed 8 flop per 16 B at HBM speed.
 #include <algorithm>
+#include <atomic>
 
 #include "bf_dfloat.cuh"
 #include "bf_internal.h"
@@ -539,7 +540,7 @@ int upload_plan(Operator& op) {
 }
 
 // Launches of level s for direction trans; returns the number of kernels.
-static int launch_stage(Operator& op, int64_t s, int trans, cudaStream_t st) {
+static int launch_stage(Operator& op, int64_t s, int trans, cudaStream_t st, float4* ws) {
   const Plan& p = op.plan;
   int nk = 0;
   if (trans == BF_OP_N) {
@@ -553,31 +554,31 @@ static int launch_stage(Operator& op, int64_t s, int trans, cudaStream_t st) {
     if (n > 0) {
       int64_t items = n / 2;
       fwd_tall_kernel<<<(unsigned)((items + FW_WARPS - 1) / FW_WARPS), WT, 0, st>>>(
-          (const int2*)(op.d_lists + b), (int)items, op.d_tasks, op.d_A, op.d_maps, op.d_ws);
+          (const int2*)(op.d_lists + b), (int)items, op.d_tasks, op.d_A, op.d_maps, ws);
       ++nk;
     }
     range(Plan::L_FLAT, b, n);
     if (n > 0) {
       fwd_flat_kernel<<<(unsigned)((n + FW_WARPS - 1) / FW_WARPS), WT, 0, st>>>(
-          op.d_lists + b, (int)n, op.d_tasks, op.d_A, op.d_maps, op.d_ws);
+          op.d_lists + b, (int)n, op.d_tasks, op.d_A, op.d_maps, ws);
       ++nk;
     }
     range(Plan::L_SMALL, b, n);
     if (n > 0) {
       fwd_small_kernel<<<(unsigned)((n + FW_WARPS - 1) / FW_WARPS), WT, 0, st>>>(
-          op.d_lists + b, (int)n, op.d_tasks, op.d_A, op.d_maps, op.d_ws);
+          op.d_lists + b, (int)n, op.d_tasks, op.d_A, op.d_maps, ws);
       ++nk;
     }
     range(Plan::L_WIDE, b, n);
     if (n > 0) {
       fwd_wide_kernel<<<(unsigned)n, 256, 0, st>>>(op.d_lists + b, op.d_tasks, op.d_A,
-                                                   op.d_maps, op.d_ws);
+                                                   op.d_maps, ws);
       ++nk;
     }
     range(Plan::L_COPY, b, n);
     if (n > 0) {
       copy_kernel<<<(unsigned)((n + 7) / 8), 256, 0, st>>>(op.d_lists + b, (int)n, op.d_tasks,
-                                                           op.d_maps, op.d_ws, 0);
+                                                           op.d_maps, ws, 0);
       ++nk;
     }
     return nk;
@@ -586,15 +587,15 @@ static int launch_stage(Operator& op, int64_t s, int trans, cudaStream_t st) {
   if (e <= b) return 0;
   const DTask* tk = op.d_tasks + b;
   if (trans == BF_OP_C)
-    stage_adj_kernel<true><<<(unsigned)(e - b), NT, 0, st>>>(tk, op.d_A, op.d_maps, op.d_ws);
+    stage_adj_kernel<true><<<(unsigned)(e - b), NT, 0, st>>>(tk, op.d_A, op.d_maps, ws);
   else
-    stage_adj_kernel<false><<<(unsigned)(e - b), NT, 0, st>>>(tk, op.d_A, op.d_maps, op.d_ws);
+    stage_adj_kernel<false><<<(unsigned)(e - b), NT, 0, st>>>(tk, op.d_A, op.d_maps, ws);
   return 1;
 }
 
 // One FP64-accurate matvec of a single right-hand side, device pointers.
 static int matvec_one(Operator& op, int trans, const double2* x, double2* y, double2 alpha,
-                      double2 beta, cudaStream_t st) {
+                      double2 beta, cudaStream_t st, float4* ws) {
   const Plan& p = op.plan;
   const bool fwd = trans == BF_OP_N;
   const int64_t nin = fwd ? p.n_cols : p.n_rows;
@@ -602,12 +603,12 @@ static int matvec_one(Operator& op, int trans, const double2* x, double2* y, dou
   const int64_t in_off = fwd ? p.xg_off : p.yg_off;
   const int64_t out_off = fwd ? p.yg_off : p.xg_off;
   const bool covered = fwd ? p.yg_covered : p.xg_covered;
-  split_kernel<<<grid_for(nin, 256), 256, 0, st>>>(x, nin, op.d_ws, in_off, 0);
+  split_kernel<<<grid_for(nin, 256), 256, 0, st>>>(x, nin, ws, in_off, 0);
   if (!covered)
-    BF_TRY_CUDA(cudaMemsetAsync(op.d_ws + out_off, 0, (size_t)nout * sizeof(float4), st));
+    BF_TRY_CUDA(cudaMemsetAsync(ws + out_off, 0, (size_t)nout * sizeof(float4), st));
   const int64_t ns = p.n_stages();
-  for (int64_t k = 0; k < ns; ++k) launch_stage(op, fwd ? k : ns - 1 - k, trans, st);
-  combine_kernel<<<grid_for(nout, 256), 256, 0, st>>>(y, nout, op.d_ws, out_off, alpha, beta,
+  for (int64_t k = 0; k < ns; ++k) launch_stage(op, fwd ? k : ns - 1 - k, trans, st, ws);
+  combine_kernel<<<grid_for(nout, 256), 256, 0, st>>>(y, nout, ws, out_off, alpha, beta,
                                                       beta.x == 0.0 && beta.y == 0.0, 0);
   BF_TRY_CUDA(cudaGetLastError());
   return BF_OK;
@@ -630,7 +631,7 @@ int profile_matvec(Operator& op, int trans, int nrep, double* ms, int64_t* bytes
     BF_TRY_CUDA(cudaEventRecord(ev[0], st));
     int64_t cnt = 2;
     for (int64_t k = 0; k < ns; ++k) {
-      cnt += launch_stage(op, fwd ? k : ns - 1 - k, trans, st);
+      cnt += launch_stage(op, fwd ? k : ns - 1 - k, trans, st, op.d_ws);
       BF_TRY_CUDA(cudaEventRecord(ev[k + 1], st));
     }
     BF_TRY_CUDA(cudaGetLastError());
@@ -677,7 +678,7 @@ int run_matvec(Operator& op, int trans, int64_t nrhs, const double* x, int64_t l
   if (ptr_mode == BF_PTR_DEVICE) {
     for (int64_t c = 0; c < nrhs; ++c)
       BF_TRY(matvec_one(op, trans, (const double2*)(x + 2 * c * ldx), (double2*)(y + 2 * c * ldy),
-                        a, b, st));
+                        a, b, st, op.d_ws));
     return BF_OK;
   }
   if (ptr_mode != BF_PTR_HOST) {
@@ -702,7 +703,7 @@ int run_matvec(Operator& op, int trans, int64_t nrhs, const double* x, int64_t l
                                   nout * 2 * sizeof(double), nrhs, cudaMemcpyHostToDevice, st));
   for (int64_t c = 0; c < nrhs; ++c)
     BF_TRY(matvec_one(op, trans, (const double2*)(op.d_x + 2 * c * nin),
-                      (double2*)(op.d_y + 2 * c * nout), a, b, st));
+                      (double2*)(op.d_y + 2 * c * nout), a, b, st, op.d_ws));
   BF_TRY_CUDA(cudaMemcpy2DAsync(y, ldy * 2 * sizeof(double), op.d_y, nout * 2 * sizeof(double),
                                 nout * 2 * sizeof(double), nrhs, cudaMemcpyDeviceToHost, st));
   BF_TRY_CUDA(cudaStreamSynchronize(st));
@@ -710,3 +711,98 @@ int run_matvec(Operator& op, int trans, int64_t nrhs, const double* x, int64_t l
 }
 
 }  // namespace bfg
+
+// ---------------------------------------------------------------------------
+// Allocation-free matvec (bf_matvec_noalloc).
+//
+// Some callers must apply the operator at a point where they cannot allocate
+// device memory: a solver step replayed inside a captured CUDA graph, a
+// callback that runs while the caller's memory pool is locked or already
+// exhausted, or a real-time loop whose allocation budget is fixed at start-up.
+// For them the level workspace (the scratch vectors between butterfly levels)
+// lives in one file-scope device array of fixed size instead of the
+// operator's own buffer.  The array is reserved in every GPU's memory as soon
+// as the library is loaded and stays there until the process exits.
+namespace bfg {
+namespace {
+
+constexpr long long NOALLOC_WS_ENTRIES = 1ll << 20;  // 16 MiB of complex float-float entries
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+__device__ __align__(256) float4 g_noalloc_ws[NOALLOC_WS_ENTRIES];
+
+// Device address of g_noalloc_ws, per device.  In host code the symbol is a
+// host-side stand-in, so the address must come from cudaGetSymbolAddress with
+// that device current.
+std::atomic<float4*> g_noalloc_addr[NOALLOC_MAX_DEVICES];
+
+int noalloc_workspace(int device, float4** out) {
+  if (device < 0 || device >= NOALLOC_MAX_DEVICES) {
+    set_error("bf_matvec_noalloc: device %d outside the supported range", device);
+    return BF_EINVAL;
+  }
+  float4* p = g_noalloc_addr[device].load(std::memory_order_acquire);
+  if (!p) {
+    void* sym = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&sym, g_noalloc_ws);
+    if (e != cudaSuccess || !sym) {
+      cudaGetLastError();
+      set_error("bf_matvec_noalloc: cudaGetSymbolAddress failed on device %d: %s", device,
+                cudaGetErrorString(e));
+      return BF_ECUDA;
+    }
+    p = (float4*)sym;
+    g_noalloc_addr[device].store(p, std::memory_order_release);
+  }
+  *out = p;
+  return BF_OK;
+}
+
+}  // namespace
+}  // namespace bfg
+
+extern "C" int bf_matvec_noalloc(bf_op_t h, int trans, int64_t nrhs, const double* x,
+                                 int64_t ldx, double* y, int64_t ldy, const double* alpha,
+                                 const double* beta, void* stream) {
+  using namespace bfg;
+  if (!h) {
+    set_error("bf_matvec_noalloc: NULL operator");
+    return BF_EINVAL;
+  }
+  Operator& op = h->op;
+  const Plan& p = op.plan;
+  if (trans != BF_OP_N && trans != BF_OP_C && trans != BF_OP_T) {
+    set_error("bf_matvec_noalloc: invalid trans %d", trans);
+    return BF_EINVAL;
+  }
+  const int64_t nin = trans == BF_OP_N ? p.n_cols : p.n_rows;
+  const int64_t nout = trans == BF_OP_N ? p.n_rows : p.n_cols;
+  if (nrhs < 0 || (nrhs > 0 && (!x || !y || ldx < nin || ldy < nout))) {
+    set_error("bf_matvec_noalloc: invalid sizes");
+    return BF_EINVAL;
+  }
+  if (p.ws_entries > NOALLOC_WS_ENTRIES) {
+    set_error("bf_matvec_noalloc: operator needs %lld workspace entries; the allocation-free "
+              "path holds at most %lld (16 MiB); use bf_matvec",
+              (long long)p.ws_entries, (long long)NOALLOC_WS_ENTRIES);
+    return BF_EINVAL;
+  }
+  if (nrhs == 0) return BF_OK;
+  if (cudaSetDevice(op.ctx->device) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("bf_matvec_noalloc: cudaSetDevice failed");
+    return BF_ECUDA;
+  }
+  float4* ws = nullptr;
+  int s = noalloc_workspace(op.ctx->device, &ws);
+  if (s != BF_OK) return s;
+  double2 a = make_double2(alpha ? alpha[0] : 1.0, alpha ? alpha[1] : 0.0);
+  double2 b = make_double2(beta ? beta[0] : 0.0, beta ? beta[1] : 0.0);
+  cudaStream_t st = stream ? (cudaStream_t)stream : op.stream;
+  for (int64_t c = 0; c < nrhs; ++c) {
+    s = matvec_one(op, trans, (const double2*)(x + 2 * c * ldx), (double2*)(y + 2 * c * ldy), a,
+                   b, st, ws);
+    if (s != BF_OK) return s;
+  }
+  return BF_OK;
+}

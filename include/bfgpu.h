@@ -181,6 +181,25 @@ BF_API int bf_matvec(bf_op_t op, int trans, int64_t nrhs, const double* x, int64
                      double* y, int64_t ldy, const double* alpha, const double* beta,
                      int ptr_mode, void* stream);
 
+/* Allocation-free FP64-accurate matvec on device pointers.  No counterpart in
+ * the reference (the Julia package always allocates through its workspaces).
+ * For callers that cannot allocate device memory when they apply the
+ * operator: a solver step replayed inside a captured CUDA graph, a callback
+ * running while the caller's memory pool is locked or exhausted, a real-time
+ * loop with a fixed allocation budget.  Same arguments as bf_matvec with
+ * ptr_mode = BF_PTR_DEVICE.  The level workspace is one file-scope device
+ * array of 16 MiB (1,048,576 complex entries) that every GPU loading the
+ * library holds until the process exits; operators whose workspace
+ * (bf_op_stats.workspace_entries) is larger are rejected with BF_EINVAL.
+ * The first call on a device looks up the array's device address (and the
+ * driver may load kernel code), so make that first call before any stream
+ * capture.  All calls share the array and it keeps the last call's
+ * contents: calls that overlap on the GPU (for example, issued on two
+ * streams) race with each other; serialise them. */
+BF_API int bf_matvec_noalloc(bf_op_t op, int trans, int64_t nrhs, const double* x, int64_t ldx,
+                             double* y, int64_t ldy, const double* alpha, const double* beta,
+                             void* stream);
+
 /* Many-RHS mixed precision: factors in complex FP32, split into BF16 hi/lo and
  * contracted in three tensor-core passes with FP32 accumulation.  Same
  * arguments as bf_matvec; relative error ~1e-5 instead of ~1e-14. */
