@@ -1,0 +1,258 @@
+// Forward level launch as a warp-specialized persistent kernel.
+//
+// One producer warp streams the column-major task matrices of a level
+// (packed back to back, see bf_pack.cpp) and the matching slices of the
+// input vector into a ring of shared-memory slots with bulk asynchronous
+// copies (cp.async.bulk = TMA without a tensor map; every task input is one
+// contiguous workspace range because the x region is stored in leaf order and
+// the level slots in reader order).  Eight consumer warps compute from shared
+// memory in float-float arithmetic and write each output entry once.  The
+// producer keeps up to TMA_NSLOT x 16 KB in flight per CTA regardless of task
+// boundaries, so the DRAM stream does not stall on per-task set-up.
+//
+// Chunks: a task with M <= TMA_SLOT rows is cut into groups of whole columns
+// (at most TMA_SLOT entries); a taller task into single-column segments of at
+// most TMA_SLOT rows, panel by panel.  Consumer mappings by M:
+//   S (M <= 32)        : G = 256/M thread groups on interleaved columns;
+//   F (32 < M <= 256)  : each warp streams a contiguous run of entries, 32
+//                        distinct rows per load, into a per-warp row
+//                        accumulator in shared memory;
+//   T (256 < M <= SLOT): thread per row, up to 4 rows per thread;
+//   P (M > SLOT)       : like T within one row panel.
+#include "bf_dfloat.cuh"
+#include "bf_internal.h"
+#include "bf_tma.cuh"
+
+namespace bfg {
+namespace {
+
+constexpr int TMA_CW = 8;                     // consumer warps
+constexpr int TMA_CT = TMA_CW * 32;           // consumer threads
+constexpr int TMA_THREADS = TMA_CT + 32;      // + one producer warp
+constexpr int TMA_SLOT = 1024;                // complex entries per matrix slot (16 KB)
+constexpr int TMA_XSLOT = 256;                // input entries per slot (4 KB)
+constexpr int TMA_NSLOT = 4;
+constexpr int TMA_FMAX = 256;                 // rows of the per-warp accumulators (mode F)
+constexpr size_t TMA_SMEM = (size_t)TMA_NSLOT * (TMA_SLOT + TMA_XSLOT) * 16 +
+                            (size_t)TMA_CW * TMA_FMAX * 16 + 2 * TMA_NSLOT * 8;
+
+struct Chunking {
+  int M, n;
+  bool panel;  // M > TMA_SLOT
+  int cpc;     // columns per chunk (column mode)
+  int np;      // row panels (panel mode)
+  __device__ void init(int m, int nn) {
+    M = m;
+    n = nn;
+    panel = M > TMA_SLOT;
+    cpc = panel ? 1 : min(TMA_XSLOT, max(1, TMA_SLOT / max(M, 1)));
+    np = panel ? (M + TMA_SLOT - 1) / TMA_SLOT : 1;
+  }
+  __device__ int count() const { return panel ? np * n : (n + cpc - 1) / cpc; }
+  // chunk k: columns [c0, c0 + cc), rows [r0, r0 + rr)
+  __device__ void get(int k, int& c0, int& cc, int& r0, int& rr) const {
+    if (panel) {
+      int p = k / n;
+      c0 = k - p * n;
+      cc = 1;
+      r0 = p * TMA_SLOT;
+      rr = min(TMA_SLOT, M - r0);
+    } else {
+      c0 = k * cpc;
+      cc = min(cpc, n - c0);
+      r0 = 0;
+      rr = M;
+    }
+  }
+};
+
+__global__ void __launch_bounds__(TMA_THREADS) fwd_tma_kernel(
+    const int32_t* __restrict__ tlist, int n_tasks, const DTask* __restrict__ tasks,
+    const float4* __restrict__ A, const int32_t* __restrict__ maps, float4* __restrict__ ws,
+    int* __restrict__ err) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  float4* sA = (float4*)smem;                                  // [NSLOT][SLOT]
+  float4* sX = sA + TMA_NSLOT * TMA_SLOT;                      // [NSLOT][XSLOT]
+  float4* sAcc = sX + TMA_NSLOT * TMA_XSLOT;                   // [CW][FMAX]
+  uint64_t* bars = (uint64_t*)(sAcc + TMA_CW * TMA_FMAX);      // full[NSLOT], empty[NSLOT]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + TMA_NSLOT);
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TMA_NSLOT; ++s) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, TMA_CW);
+    }
+    mbar_fence_init();
+  }
+  __syncthreads();
+
+  if (warp == TMA_CW) {
+    // ---------------- producer ----------------
+    if (lane != 0) return;
+    int slot = 0;
+    uint32_t ph = 0;
+    int issued[TMA_NSLOT];
+    for (int s = 0; s < TMA_NSLOT; ++s) issued[s] = -1;
+    bool ok = true;
+    for (int ti = blockIdx.x; ti < n_tasks && ok; ti += gridDim.x) {
+      const DTask t = tasks[tlist[ti]];
+      Chunking ch;
+      ch.init(t.M, t.n);
+      const int nc = ch.count();
+      for (int k = 0; k < nc; ++k) {
+        if (!mbar_wait(empty0 + 8 * slot, ph ^ 1u, err)) {
+          ok = false;
+          break;
+        }
+        int c0, cc, r0, rr;
+        ch.get(k, c0, cc, r0, rr);
+        const uint32_t abytes = (uint32_t)(cc * rr) * 16u, xbytes = (uint32_t)cc * 16u;
+        const uint32_t fb = full0 + 8 * slot;
+        fence_proxy_async();
+        mbar_arrive_expect_tx(fb, abytes + xbytes);
+        bulk_g2s(smem_u32(sA + slot * TMA_SLOT), A + t.a_off + (size_t)c0 * t.M + r0, abytes, fb);
+        bulk_g2s(smem_u32(sX + slot * TMA_XSLOT), ws + t.cbase + c0, xbytes, fb);
+        issued[slot] = (int)ph;
+        if (++slot == TMA_NSLOT) {
+          slot = 0;
+          ph ^= 1u;
+        }
+      }
+    }
+    // no copy may still be in flight when the block exits
+    for (int s = 0; s < TMA_NSLOT; ++s)
+      if (issued[s] >= 0) mbar_wait_drain(full0 + 8 * s, (uint32_t)issued[s], err);
+    return;
+  }
+
+  // ---------------- consumers ----------------
+  const int tid = threadIdx.x;  // < TMA_CT
+  float4* accw = sAcc + warp * TMA_FMAX;
+  int slot = 0;
+  uint32_t ph = 0;
+  // after a failed wait a warp keeps walking the same task/chunk sequence
+  // (and the same named barriers) without touching data, so no warp can be
+  // left waiting at a barrier
+  bool dead = false;
+  for (int i = lane; i < TMA_FMAX; i += 32) accw[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  __syncwarp();
+  for (int ti = blockIdx.x; ti < n_tasks; ti += gridDim.x) {
+    const DTask t = tasks[tlist[ti]];
+    const int32_t* __restrict__ rmap = maps + t.rmap_off;
+    const int M = t.M, n = t.n;
+    Chunking ch;
+    ch.init(M, n);
+    const int nc = ch.count();
+    const int mode = M <= 32 ? 0 : (M <= TMA_FMAX ? 1 : 2);  // S, F, T/P
+    const int G = mode == 0 ? TMA_CT / M : 1;
+    const int g = mode == 0 ? tid / M : 0;
+    const int gi = mode == 0 ? tid - g * M : 0;
+    float4 acc[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int k = 0; k < nc; ++k) {
+      bool got = dead ? false : mbar_wait(full0 + 8 * slot, ph, err);
+      dead = __any_sync(0xffffffffu, !got);
+      int c0, cc, r0, rr;
+      ch.get(k, c0, cc, r0, rr);
+      const float4* __restrict__ a = sA + slot * TMA_SLOT;
+      const float4* __restrict__ xv = sX + slot * TMA_XSLOT;
+      if (dead) {
+        // skip the data; still release the slot below
+      } else if (mode == 0) {
+        if (g < G)
+          for (int c = g; c < cc; c += G) cdf_mac(acc[0], a[c * M + gi], xv[c]);
+      } else if (mode == 1) {
+        const int E = cc * M;
+        const int per = (E + TMA_CW - 1) / TMA_CW;
+        const int e0 = warp * per, e1 = min(E, e0 + per);
+        int e = e0 + lane;
+        int col = e / M, row = e - col * M;
+        for (; e < e1; e += 32) {
+          float4 s = accw[row];
+          cdf_mac(s, a[e], xv[col]);
+          accw[row] = s;
+          row += 32;
+          if (row >= M) {
+            row -= M;
+            ++col;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int i = tid + q * TMA_CT;
+          if (i < rr)
+            for (int c = 0; c < cc; ++c) cdf_mac(acc[q], a[c * rr + i], xv[c]);
+        }
+        if (ch.panel && c0 == n - 1) {  // end of a row panel: flush its rows
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int i = tid + q * TMA_CT;
+            if (i < rr) ws[rmap[r0 + i]] = cdf_norm(acc[q]);
+            acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+        }
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(empty0 + 8 * slot);
+      if (++slot == TMA_NSLOT) {
+        slot = 0;
+        ph ^= 1u;
+      }
+    }
+    // ---- task epilogue: reduce partial sums and write each output once
+    if (mode == 0) {
+      named_sync(TMA_CT);
+      float4* red = sAcc;  // reuse the accumulator area (G*M <= 256 entries)
+      if (g < G) red[tid] = acc[0];
+      named_sync(TMA_CT);
+      if (tid < M) {
+        float4 v = red[tid];
+        for (int q = 1; q < G; ++q) cdf_add(v, red[q * M + tid]);
+        ws[rmap[tid]] = cdf_norm(v);
+      }
+      named_sync(TMA_CT);
+      for (int i = lane; i < TMA_FMAX; i += 32) accw[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+      named_sync(TMA_CT);
+    } else if (mode == 1) {
+      named_sync(TMA_CT);
+      if (tid < M) {
+        float4 v = sAcc[tid];
+        for (int w = 1; w < TMA_CW; ++w) cdf_add(v, sAcc[w * TMA_FMAX + tid]);
+        ws[rmap[tid]] = cdf_norm(v);
+      }
+      named_sync(TMA_CT);
+      for (int i = lane; i < M; i += 32) accw[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+      __syncwarp();
+    } else if (!ch.panel) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int i = tid + q * TMA_CT;
+        if (i < M) ws[rmap[i]] = cdf_norm(acc[q]);
+      }
+    } else if (n == 0) {
+      for (int i = tid; i < M; i += TMA_CT) ws[rmap[i]] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
+}
+
+}  // namespace
+
+int launch_fwd_tma(const int32_t* d_tlist, int n_tasks, const DTask* d_tasks, const float4* d_A,
+                   const int32_t* d_maps, float4* d_ws, int* d_err, int n_sm, cudaStream_t st) {
+  if (n_tasks <= 0) return BF_OK;
+  static bool attr = false;
+  if (!attr) {
+    BF_TRY_CUDA(cudaFuncSetAttribute(fwd_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)TMA_SMEM));
+    attr = true;
+  }
+  int grid = std::min(n_tasks, 2 * n_sm);
+  fwd_tma_kernel<<<grid, TMA_THREADS, TMA_SMEM, st>>>(d_tlist, n_tasks, d_tasks, d_A, d_maps,
+                                                        d_ws, d_err);
+  BF_TRY_CUDA(cudaGetLastError());
+  return BF_OK;
+}
+
+}  // namespace bfg

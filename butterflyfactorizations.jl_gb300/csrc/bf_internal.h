@@ -82,7 +82,9 @@ struct Logical {
 enum : int32_t { TASK_DENSE = 0, TASK_COPY = 1 };
 
 // task shape classes of the forward kernels
-constexpr int TALL_ROWS = 128;  // rows per tall-kernel warp item
+constexpr int TALL_ROWS = 128;  // rows per tall-kernel panel
+constexpr int TALL_PANELS = 1;  // panels per tall-kernel warp item
+constexpr int WIDE_NMIN = 128;  // wide class: M <= 32, n > 2M and n >= WIDE_NMIN
 constexpr int FLAT_MMAX = 128;  // flat kernel: 32 < M <= FLAT_MMAX
 constexpr int FLAT_NMAX = 256;  //              n <= FLAT_NMAX
 
@@ -92,7 +94,10 @@ struct alignas(16) DTask {
   long long a_off;     // first complex entry of the M x n column-major matrix
   long long rmap_off;  // offset into the routing array
   long long cmap_off;
-  int M, n, kind, pad;
+  int M, n, kind;
+  int cbase;  // workspace offset of column j is cbase + j (contiguous), else -1
+  int rbase;  // same for the rows
+  int pad;
 };
 static_assert(sizeof(DTask) == 48, "DTask layout");
 
@@ -109,6 +114,9 @@ static_assert(sizeof(DSeg) == 48, "DSeg layout");
 struct Plan {
   int64_t n_rows = 0, n_cols = 0;
   int64_t xg_off = 0, yg_off = 0;  // x-space and y-space regions of the workspace
+  // the x / y regions hold points in leaf order: region entry q is point xperm[q]
+  // (yperm[q]), so every leaf's values are one contiguous range
+  std::vector<int32_t> xperm, yperm;
   int64_t ws_entries = 0;
   std::vector<DTask> tasks;
   std::vector<int64_t> stage_begin;  // n_stages + 1
@@ -116,9 +124,11 @@ struct Plan {
   // forward launch lists (one per task shape class, see bf_matvec.cu), all
   // concatenated in `lists`; begin[c][s] indexes class c at stage s (in
   // entries; tall items are (task, row0) pairs and count two entries each)
-  enum { L_TALL = 0, L_FLAT, L_SMALL, L_WIDE, L_COPY, L_NCLASS };
+  enum { L_TALL = 0, L_FLAT, L_SMALL, L_WIDE, L_COPY, L_DENSE, L_NCLASS };
   std::vector<int32_t> lists;
   std::vector<int64_t> list_begin[L_NCLASS];  // n_stages + 1 each
+  // stage s can use the bulk-copy pipeline (every dense task input contiguous)
+  std::vector<uint8_t> stage_tma;
   std::vector<int32_t> maps;
   int64_t a_entries = 0;
   std::vector<DSeg> segs;
@@ -152,6 +162,10 @@ struct Operator {
   int32_t* d_maps = nullptr;
   float4* d_ws = nullptr;
   int32_t* d_lists = nullptr;  // forward launch lists (Plan::lists)
+  int32_t* d_xperm = nullptr;  // leaf order of the x / y regions (Plan::xperm, yperm)
+  int32_t* d_yperm = nullptr;
+  int* d_err = nullptr;        // device error word of bounded waits (0 = ok)
+  int fwd_kernel = 0;          // 0 = bulk-copy pipeline where possible, 1 = direct loads
   // staging of host right-hand sides
   double* d_x = nullptr;
   double* d_y = nullptr;
@@ -177,6 +191,8 @@ int build_operator(Context* ctx, const double* obs_xyz, int64_t n_obs, const dou
                    const bf_build_opts& opts, Operator& op);
 int profile_matvec(Operator& op, int trans, int nrep, double* ms, int64_t* bytes,
                    int64_t* kernels);
+int launch_fwd_tma(const int32_t* d_tlist, int n_tasks, const DTask* d_tasks, const float4* d_A,
+                   const int32_t* d_maps, float4* d_ws, int* d_err, int n_sm, cudaStream_t st);
 int run_matvec(Operator& op, int trans, int64_t nrhs, const double* x, int64_t ldx, double* y,
                int64_t ldy, const double* alpha, const double* beta, int ptr_mode,
                cudaStream_t stream);

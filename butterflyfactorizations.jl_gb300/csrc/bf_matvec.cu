@@ -13,6 +13,8 @@
 // rate (about 1.2 TFLOP/s) cannot feed 8 flop per 16 B at HBM speed.
 #include <algorithm>
 #include <atomic>
+#include <cstdlib>
+#include <string>
 
 #include "bf_dfloat.cuh"
 #include "bf_internal.h"
@@ -186,12 +188,13 @@ __global__ void repack_kernel(const DSeg* __restrict__ segs, const SrcT* __restr
   }
 }
 
-// x (complex double, n entries) -> ws[off + i] (complex float-float); optional conj
+// x (complex double, n entries) -> ws[off + q] = split(x[perm[q]]) (complex
+// float-float, leaf order); optional conj
 __global__ void split_kernel(const double2* __restrict__ x, int64_t n, float4* __restrict__ ws,
-                             int64_t off, int conj) {
+                             int64_t off, int conj, const int32_t* __restrict__ perm) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    double2 v = x[i];
+    double2 v = x[perm ? perm[i] : i];
     float2 re = df_split(v.x), im = df_split(conj ? -v.y : v.y);
     ws[off + i] = make_float4(re.x, re.y, im.x, im.y);
   }
@@ -200,10 +203,11 @@ __global__ void split_kernel(const double2* __restrict__ x, int64_t n, float4* _
 // y = beta*y + alpha*v, v = ws[off + i] (optionally conjugated first)
 __global__ void combine_kernel(double2* __restrict__ y, int64_t n, const float4* __restrict__ ws,
                                int64_t off, double2 alpha, double2 beta, int beta_zero,
-                               int conj) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    float4 a = ws[off + i];
+                               int conj, const int32_t* __restrict__ perm) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = perm ? perm[q] : q;  // region entry q is point perm[q]
+    float4 a = ws[off + q];
     double vr = (double)a.x + (double)a.y;
     double vi = (double)a.z + (double)a.w;
     if (conj) vi = -vi;
@@ -244,18 +248,30 @@ __global__ void __launch_bounds__(FW_WARPS * 32) fwd_tall_kernel(
   const DTask t = tasks[it.x];
   const int32_t* __restrict__ rmap = maps + t.rmap_off;
   const int32_t* __restrict__ cmap = maps + t.cmap_off;
-  const int M = t.M, n = t.n, r0 = it.y;
+  const int M = t.M, n = t.n;
+  float4* __restrict__ xw = xs[warp];
+  // an item covers TALL_PANELS row panels of TALL_ROWS rows; the input block
+  // is staged once when it fits (n <= FW_XB, the Q-stage case)
+  const bool one_block = n <= FW_XB;
+  if (one_block) {
+    for (int j = lane; j < n; j += 32) xw[j] = t.cbase >= 0 ? ws[t.cbase + j] : ws[cmap[j]];
+    __syncwarp();
+  }
+  for (int pnl = 0; pnl < TALL_PANELS; ++pnl) {
+  const int r0 = it.y + pnl * TALL_ROWS;
+  if (r0 >= M) break;
   float4 acc[TALL_RPL];
 #pragma unroll
   for (int q = 0; q < TALL_RPL; ++q) acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
   bool act[TALL_RPL];
 #pragma unroll
   for (int q = 0; q < TALL_RPL; ++q) act[q] = r0 + lane + 32 * q < M;
-  float4* __restrict__ xw = xs[warp];
   for (int cb = 0; cb < n; cb += FW_XB) {
     const int nb = min(FW_XB, n - cb);
-    for (int j = lane; j < nb; j += 32) xw[j] = ws[cmap[cb + j]];
-    __syncwarp();
+    if (!one_block) {
+      for (int j = lane; j < nb; j += 32) xw[j] = t.cbase >= 0 ? ws[t.cbase + cb + j] : ws[cmap[cb + j]];
+      __syncwarp();
+    }
     const float4* __restrict__ ap = A + t.a_off + (size_t)cb * M + r0 + lane;
     int j = 0;
     for (; j + 1 < nb; j += 2) {  // 2 columns x 4 rows: eight loads in flight
@@ -284,6 +300,7 @@ __global__ void __launch_bounds__(FW_WARPS * 32) fwd_tall_kernel(
 #pragma unroll
   for (int q = 0; q < TALL_RPL; ++q)
     if (act[q]) ws[rmap[r0 + lane + 32 * q]] = cdf_norm(acc[q]);
+  }  // panels
 }
 
 // One warp streams a whole task flat: lane l reads entry e = l + 32k of the
@@ -304,7 +321,7 @@ __global__ void __launch_bounds__(FW_WARPS * 32) fwd_flat_kernel(
   const int M = t.M, n = t.n;
   float4* __restrict__ xw = xs[warp];
   float4* __restrict__ aw = as[warp];
-  for (int j = lane; j < n; j += 32) xw[j] = ws[cmap[j]];
+  for (int j = lane; j < n; j += 32) xw[j] = t.cbase >= 0 ? ws[t.cbase + j] : ws[cmap[j]];
   for (int i = lane; i < M; i += 32) aw[i] = make_float4(0.f, 0.f, 0.f, 0.f);
   __syncwarp();
   const long long tot = (long long)M * n;
@@ -361,7 +378,7 @@ __global__ void __launch_bounds__(FW_WARPS * 32) fwd_small_kernel(
   float4* __restrict__ xw = xs[warp];
   for (int cb = 0; cb < n; cb += FW_XB) {
     const int nb = min(FW_XB, n - cb);
-    for (int j = lane; j < nb; j += 32) xw[j] = ws[cmap[cb + j]];
+    for (int j = lane; j < nb; j += 32) xw[j] = t.cbase >= 0 ? ws[t.cbase + cb + j] : ws[cmap[cb + j]];
     __syncwarp();
     if (active) {
       const size_t step = (size_t)G * M;
@@ -478,6 +495,9 @@ Operator::~Operator() {
   if (d_maps) cudaFree(d_maps);
   if (d_ws) cudaFree(d_ws);
   if (d_lists) cudaFree(d_lists);
+  if (d_err) cudaFree(d_err);
+  if (d_xperm) cudaFree(d_xperm);
+  if (d_yperm) cudaFree(d_yperm);
   if (d_x) cudaFree(d_x);
   if (d_y) cudaFree(d_y);
   if (stream) cudaStreamDestroy(stream);
@@ -523,6 +543,20 @@ int upload_plan(Operator& op) {
     return BF_ENOMEM;
   }
   BF_TRY_CUDA(cudaMemset(op.d_ws, 0, (size_t)std::max<int64_t>(p.ws_entries, 1) * sizeof(float4)));
+  BF_TRY_CUDA(cudaMalloc(&op.d_err, sizeof(int)));
+  BF_TRY_CUDA(cudaMemset(op.d_err, 0, sizeof(int)));
+  {
+    // forward kernel family: the bulk-copy pipeline unless the caller asks for
+    // the direct-load kernels (used to compare the two in benchmarks)
+    const char* fk = getenv("BFGPU_FWD_KERNEL");
+    op.fwd_kernel = (fk && std::string(fk) == "direct") ? 1 : 0;
+  }
+  BF_TRY_CUDA(cudaMalloc(&op.d_xperm, std::max<size_t>(1, p.xperm.size()) * sizeof(int32_t)));
+  BF_TRY_CUDA(cudaMemcpy(op.d_xperm, p.xperm.data(), p.xperm.size() * sizeof(int32_t),
+                         cudaMemcpyHostToDevice));
+  BF_TRY_CUDA(cudaMalloc(&op.d_yperm, std::max<size_t>(1, p.yperm.size()) * sizeof(int32_t)));
+  BF_TRY_CUDA(cudaMemcpy(op.d_yperm, p.yperm.data(), p.yperm.size() * sizeof(int32_t),
+                         cudaMemcpyHostToDevice));
   BF_TRY_CUDA(cudaMalloc(&op.d_lists, std::max<size_t>(1, p.lists.size()) * sizeof(int32_t)));
   if (!p.lists.empty())
     BF_TRY_CUDA(cudaMemcpy(op.d_lists, p.lists.data(), p.lists.size() * sizeof(int32_t),
@@ -550,6 +584,9 @@ static int launch_stage(Operator& op, int64_t s, int trans, cudaStream_t st, flo
     };
     int64_t b, n;
     const unsigned WT = FW_WARPS * 32;
+    // short wide tasks (the P stage) stream through the bulk-copy pipeline; the
+    // many small R-level tasks and the tall Q tasks run the direct-load kernels
+    const bool tma_wide = p.stage_tma[s] && op.fwd_kernel == 0;
     range(Plan::L_TALL, b, n);
     if (n > 0) {
       int64_t items = n / 2;
@@ -570,7 +607,11 @@ static int launch_stage(Operator& op, int64_t s, int trans, cudaStream_t st, flo
       ++nk;
     }
     range(Plan::L_WIDE, b, n);
-    if (n > 0) {
+    if (n > 0 && tma_wide) {
+      BF_TRY(launch_fwd_tma(op.d_lists + b, (int)n, op.d_tasks, op.d_A, op.d_maps, ws, op.d_err,
+                            op.ctx->prop.multiProcessorCount, st));
+      ++nk;
+    } else if (n > 0) {
       fwd_wide_kernel<<<(unsigned)n, 256, 0, st>>>(op.d_lists + b, op.d_tasks, op.d_A,
                                                    op.d_maps, ws);
       ++nk;
@@ -603,13 +644,15 @@ static int matvec_one(Operator& op, int trans, const double2* x, double2* y, dou
   const int64_t in_off = fwd ? p.xg_off : p.yg_off;
   const int64_t out_off = fwd ? p.yg_off : p.xg_off;
   const bool covered = fwd ? p.yg_covered : p.xg_covered;
-  split_kernel<<<grid_for(nin, 256), 256, 0, st>>>(x, nin, ws, in_off, 0);
+  split_kernel<<<grid_for(nin, 256), 256, 0, st>>>(x, nin, ws, in_off, 0,
+                                                    fwd ? op.d_xperm : op.d_yperm);
   if (!covered)
     BF_TRY_CUDA(cudaMemsetAsync(ws + out_off, 0, (size_t)nout * sizeof(float4), st));
   const int64_t ns = p.n_stages();
   for (int64_t k = 0; k < ns; ++k) launch_stage(op, fwd ? k : ns - 1 - k, trans, st, ws);
   combine_kernel<<<grid_for(nout, 256), 256, 0, st>>>(y, nout, ws, out_off, alpha, beta,
-                                                      beta.x == 0.0 && beta.y == 0.0, 0);
+                                                      beta.x == 0.0 && beta.y == 0.0, 0,
+                                                      fwd ? op.d_yperm : op.d_xperm);
   BF_TRY_CUDA(cudaGetLastError());
   return BF_OK;
 }

@@ -324,8 +324,44 @@ int pack_plan(const Logical& lg, Plan& plan) {
     return BF_ENOTSUP;
   }
 
+  // ---- leaf order of the x and y regions: the points of each Q-stage source
+  // leaf (P-stage observer leaf) become one contiguous range
+  std::vector<int64_t> xpos(lg.n_cols, -1), ypos(lg.n_rows, -1);
+  {
+    int64_t nx = 0, ny = 0;
+    for (auto& t : stages[0])
+      for (auto& c : t.cols)
+        if (c.type == SIDE_X) {
+          const int64_t* v = lg.src_vals.v(c.id);
+          for (int64_t i = 0; i < c.len; ++i)
+            if (xpos[v[i]] < 0) xpos[v[i]] = nx++;
+        }
+    for (auto& t : stages[Lmax])
+      for (auto& r : t.rows)
+        if (r.type == SIDE_Y) {
+          const int64_t* v = lg.obs_vals.v(r.id);
+          for (int64_t i = 0; i < r.len; ++i)
+            if (ypos[v[i]] < 0) ypos[v[i]] = ny++;
+        }
+    for (int64_t p = 0; p < lg.n_cols; ++p)
+      if (xpos[p] < 0) xpos[p] = nx++;
+    for (int64_t p = 0; p < lg.n_rows; ++p)
+      if (ypos[p] < 0) ypos[p] = ny++;
+    plan.xperm.assign(lg.n_cols, 0);
+    plan.yperm.assign(lg.n_rows, 0);
+    for (int64_t p = 0; p < lg.n_cols; ++p) plan.xperm[xpos[p]] = (int32_t)p;
+    for (int64_t p = 0; p < lg.n_rows; ++p) plan.yperm[ypos[p]] = (int32_t)p;
+  }
+
   // ---- emit tasks, maps, repack segments
   std::vector<uint8_t> ycov(lg.n_rows, 0), xcov(lg.n_cols, 0);
+  auto contiguous_base = [&](int64_t off, int64_t len) -> int {
+    if (len <= 0) return -1;
+    int32_t b = plan.maps[off];
+    for (int64_t i = 1; i < len; ++i)
+      if (plan.maps[off + i] != b + i) return -1;
+    return b;
+  };
   plan.stage_begin.push_back(0);
   int64_t a_off = 0;
   int64_t alg = 0;
@@ -348,13 +384,13 @@ int pack_plan(const Logical& lg, Plan& plan) {
         } else if (sd.type == SIDE_X) {
           const int64_t* v = lg.src_vals.v(sd.id);
           for (int64_t i = 0; i < sd.len; ++i) {
-            plan.maps.push_back((int32_t)(plan.xg_off + v[i]));
+            plan.maps.push_back((int32_t)(plan.xg_off + xpos[v[i]]));
             xcov[v[i]] = 1;
           }
         } else {
           const int64_t* v = lg.obs_vals.v(sd.id);
           for (int64_t i = 0; i < sd.len; ++i) {
-            plan.maps.push_back((int32_t)(plan.yg_off + v[i]));
+            plan.maps.push_back((int32_t)(plan.yg_off + ypos[v[i]]));
             if (ycov[v[i]]) {
               set_error("pack: output row %lld written by two P tasks", (long long)v[i]);
               throw BF_EINVAL;
@@ -371,6 +407,8 @@ int pack_plan(const Logical& lg, Plan& plan) {
       } catch (int code) {
         return code;
       }
+      d.rbase = contiguous_base(d.rmap_off, t.M);
+      d.cbase = contiguous_base(d.cmap_off, t.n);
       if (t.kind == TASK_DENSE) {
         d.a_off = a_off;
         for (auto& m : t.mats) {
@@ -413,22 +451,29 @@ int pack_plan(const Logical& lg, Plan& plan) {
       for (int64_t gi = plan.stage_begin[s]; gi < plan.stage_begin[s + 1]; ++gi) {
         const DTask& d = plan.tasks[gi];
         if (d.M <= 0) continue;
+        if (d.kind == TASK_DENSE) cls[Plan::L_DENSE].push_back((int32_t)gi);
         if (d.kind == TASK_COPY) {
           cls[Plan::L_COPY].push_back((int32_t)gi);
-        } else if (d.M <= 32 && d.n > 2 * d.M) {
+        } else if (d.M <= 32 && d.n > 2 * d.M && d.n >= WIDE_NMIN) {
           cls[Plan::L_WIDE].push_back((int32_t)gi);
         } else if (d.M <= 32) {
           cls[Plan::L_SMALL].push_back((int32_t)gi);
         } else if (d.M <= FLAT_MMAX && d.n <= FLAT_NMAX) {
           cls[Plan::L_FLAT].push_back((int32_t)gi);
         } else {
-          for (int32_t r0 = 0; r0 < d.M; r0 += TALL_ROWS) {
+          for (int32_t r0 = 0; r0 < d.M; r0 += TALL_ROWS * TALL_PANELS) {
             cls[Plan::L_TALL].push_back((int32_t)gi);
             cls[Plan::L_TALL].push_back(r0);
           }
         }
       }
       for (int c = 0; c < Plan::L_NCLASS; ++c) ends[c].push_back((int64_t)cls[c].size());
+      bool tma = true;
+      for (int64_t gi = plan.stage_begin[s]; gi < plan.stage_begin[s + 1]; ++gi) {
+        const DTask& d = plan.tasks[gi];
+        if (d.kind == TASK_DENSE && d.M > 0 && d.n > 0 && d.cbase < 0) tma = false;
+      }
+      plan.stage_tma.push_back(tma ? 1 : 0);
     }
     // concatenate; list_begin holds absolute offsets into plan.lists
     for (int c = 0; c < Plan::L_NCLASS; ++c) {
