@@ -82,7 +82,7 @@ struct Logical {
 enum : int32_t { TASK_DENSE = 0, TASK_COPY = 1 };
 
 // task shape classes of the forward kernels
-constexpr int TALL_ROWS = 128;  // rows per tall-kernel panel
+constexpr int TALL_ROWS = 64;   // rows per tall-kernel panel
 constexpr int TALL_PANELS = 1;  // panels per tall-kernel warp item
 constexpr int WIDE_NMIN = 128;  // wide class: M <= 32, n > 2M and n >= WIDE_NMIN
 constexpr int FLAT_MMAX = 128;  // flat kernel: 32 < M <= FLAT_MMAX

@@ -274,20 +274,28 @@ __global__ void __launch_bounds__(FW_WARPS * 32) fwd_tall_kernel(
     }
     const float4* __restrict__ ap = A + t.a_off + (size_t)cb * M + r0 + lane;
     int j = 0;
-    for (; j + 1 < nb; j += 2) {  // 2 columns x 4 rows: eight loads in flight
-      float4 a[2][TALL_RPL];
+    constexpr int CPI = 8 / TALL_RPL;  // columns per iteration: eight loads in flight
+    for (; j + CPI - 1 < nb; j += CPI) {
+      float4 a[CPI][TALL_RPL];
 #pragma unroll
-      for (int c = 0; c < 2; ++c)
+      for (int c = 0; c < CPI; ++c)
 #pragma unroll
         for (int q = 0; q < TALL_RPL; ++q)
           a[c][q] = act[q] ? __ldg(ap + (size_t)c * M + 32 * q) : make_float4(0.f, 0.f, 0.f, 0.f);
-      const float4 x0 = xw[j], x1 = xw[j + 1];
 #pragma unroll
-      for (int q = 0; q < TALL_RPL; ++q) {
-        cdf_mac(acc[q], a[0][q], x0);
-        cdf_mac(acc[q], a[1][q], x1);
+      for (int c = 0; c < CPI; ++c) {
+        const float4 xc = xw[j + c];
+#pragma unroll
+        for (int q = 0; q < TALL_RPL; ++q) cdf_mac(acc[q], a[c][q], xc);
       }
-      ap += 2 * (size_t)M;
+      ap += CPI * (size_t)M;
+    }
+    for (; j + 1 < nb; j += 1) {
+      const float4 x0 = xw[j];
+#pragma unroll
+      for (int q = 0; q < TALL_RPL; ++q)
+        if (act[q]) cdf_mac(acc[q], __ldg(ap + 32 * q), x0);
+      ap += M;
     }
     if (j < nb) {
       const float4 x0 = xw[j];
