@@ -85,6 +85,7 @@ enum : int32_t { TASK_DENSE = 0, TASK_COPY = 1 };
 constexpr int TALL_ROWS = 64;   // rows per tall-kernel panel
 constexpr int TALL_PANELS = 1;  // panels per tall-kernel warp item
 constexpr int WIDE_NMIN = 128;  // wide class: M <= 32, n > 2M and n >= WIDE_NMIN
+constexpr int ADJ_TALL_M = 128; // adjoint: tasks with more rows get a CTA each
 constexpr int FLAT_MMAX = 128;  // flat kernel: 32 < M <= FLAT_MMAX
 constexpr int FLAT_NMAX = 256;  //              n <= FLAT_NMAX
 
@@ -124,7 +125,9 @@ struct Plan {
   // forward launch lists (one per task shape class, see bf_matvec.cu), all
   // concatenated in `lists`; begin[c][s] indexes class c at stage s (in
   // entries; tall items are (task, row0) pairs and count two entries each)
-  enum { L_TALL = 0, L_FLAT, L_SMALL, L_WIDE, L_COPY, L_DENSE, L_NCLASS };
+  // L_ATALL / L_AWARP: adjoint CTA-per-task (M > ADJ_TALL_M) and warp-per-task
+  // lists (the adjoint shares L_WIDE and L_COPY with the forward)
+  enum { L_TALL = 0, L_FLAT, L_SMALL, L_WIDE, L_COPY, L_DENSE, L_ATALL, L_AWARP, L_NCLASS };
   std::vector<int32_t> lists;
   std::vector<int64_t> list_begin[L_NCLASS];  // n_stages + 1 each
   // stage s can use the bulk-copy pipeline (every dense task input contiguous)
@@ -193,6 +196,10 @@ int profile_matvec(Operator& op, int trans, int nrep, double* ms, int64_t* bytes
                    int64_t* kernels);
 int launch_fwd_tma(const int32_t* d_tlist, int n_tasks, const DTask* d_tasks, const float4* d_A,
                    const int32_t* d_maps, float4* d_ws, int* d_err, int n_sm, cudaStream_t st);
+// adjoint (conj) / transpose launches of level s; returns the kernel count or -1
+int launch_adj_stage(const Plan& p, int64_t s, bool conj, const int32_t* d_lists,
+                     const DTask* d_tasks, const float4* d_A, const int32_t* d_maps,
+                     float4* d_ws, cudaStream_t st);
 int run_matvec(Operator& op, int trans, int64_t nrhs, const double* x, int64_t ldx, double* y,
                int64_t ldy, const double* alpha, const double* beta, int ptr_mode,
                cudaStream_t stream);

@@ -632,14 +632,17 @@ static int launch_stage(Operator& op, int64_t s, int trans, cudaStream_t st, flo
     }
     return nk;
   }
-  int64_t b = p.stage_begin[s], e = p.stage_begin[s + 1];
-  if (e <= b) return 0;
-  const DTask* tk = op.d_tasks + b;
-  if (trans == BF_OP_C)
-    stage_adj_kernel<true><<<(unsigned)(e - b), NT, 0, st>>>(tk, op.d_A, op.d_maps, ws);
-  else
-    stage_adj_kernel<false><<<(unsigned)(e - b), NT, 0, st>>>(tk, op.d_A, op.d_maps, ws);
-  return 1;
+  // adjoint / transpose: same tasks, rows and columns swapped
+  nk = launch_adj_stage(p, s, trans == BF_OP_C, op.d_lists, op.d_tasks, op.d_A, op.d_maps, ws,
+                        st);
+  if (nk < 0) return 0;
+  int64_t b = p.list_begin[Plan::L_COPY][s], n = p.list_begin[Plan::L_COPY][s + 1] - b;
+  if (n > 0) {
+    copy_kernel<<<(unsigned)((n + 7) / 8), 256, 0, st>>>(op.d_lists + b, (int)n, op.d_tasks,
+                                                         op.d_maps, ws, 1);
+    ++nk;
+  }
+  return nk;
 }
 
 // One FP64-accurate matvec of a single right-hand side, device pointers.

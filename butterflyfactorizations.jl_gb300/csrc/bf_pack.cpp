@@ -450,6 +450,16 @@ int pack_plan(const Logical& lg, Plan& plan) {
     for (int64_t s = 0; s + 1 < (int64_t)plan.stage_begin.size(); ++s) {
       for (int64_t gi = plan.stage_begin[s]; gi < plan.stage_begin[s + 1]; ++gi) {
         const DTask& d = plan.tasks[gi];
+        // adjoint lists (a task with no rows still writes zeros to its columns)
+        if (d.kind == TASK_DENSE && d.n > 0) {
+          if (d.M <= 32 && d.n > 2 * d.M && d.n >= WIDE_NMIN) {
+            // served by L_WIDE below
+          } else if (d.M > ADJ_TALL_M) {
+            cls[Plan::L_ATALL].push_back((int32_t)gi);
+          } else {
+            cls[Plan::L_AWARP].push_back((int32_t)gi);
+          }
+        }
         if (d.M <= 0) continue;
         if (d.kind == TASK_DENSE) cls[Plan::L_DENSE].push_back((int32_t)gi);
         if (d.kind == TASK_COPY) {
