@@ -297,6 +297,26 @@ class Operator:
                                 _p(by, C.c_int64), C.byref(nk)), "bf_op_profile")
         return ms, by, nk.value
 
+    def profile_mixed(self, nrep: int = 3):
+        """Mixed path, one 128-RHS chunk: per-level ms, bytes, useful flops, kernels."""
+        lib = load()
+        ns = self.stats()["n_stages"]
+        ms = np.zeros(ns)
+        by = np.zeros(ns, np.int64)
+        fl = np.zeros(ns)
+        nk = C.c_int64()
+        check(lib.bf_op_profile_mixed(self._h, self.trans, int(nrep), _p(ms, C.c_double),
+                                      _p(by, C.c_int64), _p(fl, C.c_double), C.byref(nk)),
+              "bf_op_profile_mixed")
+        return ms, by, fl, nk.value
+
+    def mixed_info(self) -> dict:
+        """BF16 factor bytes, workspace bytes and work units of the mixed path."""
+        f, w, u = C.c_int64(), C.c_int64(), C.c_int64()
+        check(load().bf_op_mixed_info(self._h, C.byref(f), C.byref(w), C.byref(u)),
+              "bf_op_mixed_info")
+        return dict(factor_bytes=f.value, workspace_bytes=w.value, work_units=u.value)
+
     def close(self):
         if self._parent is None and self._h and self._h.value:
             load().bf_op_destroy(self._h)

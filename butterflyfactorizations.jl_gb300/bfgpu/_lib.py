@@ -68,6 +68,8 @@ SIGNATURES = [
                                       P(i64), vp, i32]),
     ("bf_op_rank_log", C.c_int, [vp, P(i64), P(f64)]),
     ("bf_op_profile", C.c_int, [vp, C.c_int, i32, P(f64), P(i64), P(i64)]),
+    ("bf_op_profile_mixed", C.c_int, [vp, C.c_int, i32, P(f64), P(i64), P(f64), P(i64)]),
+    ("bf_op_mixed_info", C.c_int, [vp, P(i64), P(i64), P(i64)]),
     ("bf_op_task_shapes", C.c_int, [vp, P(i64), P(i32), P(i32), P(i32), P(i32)]),
     ("bf_op_destroy", C.c_int, [vp]),
 ]

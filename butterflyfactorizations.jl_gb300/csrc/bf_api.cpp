@@ -227,6 +227,44 @@ int bf_matvec(bf_op_t op, int trans, int64_t nrhs, const double* x, int64_t ldx,
   BF_GUARD_END
 }
 
+int bf_matvec_mixed(bf_op_t op, int trans, int64_t nrhs, const double* x, int64_t ldx, double* y,
+                    int64_t ldy, const double* alpha, const double* beta, int ptr_mode,
+                    void* stream) {
+  BF_GUARD_BEGIN
+  if (!op) {
+    set_error("bf_matvec_mixed: NULL operator");
+    return BF_EINVAL;
+  }
+  return run_matvec_mixed(op->op, trans, nrhs, x, ldx, y, ldy, alpha, beta, ptr_mode,
+                          (cudaStream_t)stream);
+  BF_GUARD_END
+}
+
+int bf_op_profile_mixed(bf_op_t op, int trans, int32_t nrep, double* ms, int64_t* bytes,
+                        double* flops, int64_t* kernels) {
+  BF_GUARD_BEGIN
+  if (!op) {
+    set_error("bf_op_profile_mixed: NULL operator");
+    return BF_EINVAL;
+  }
+  if (trans != BF_OP_N && trans != BF_OP_C && trans != BF_OP_T) {
+    set_error("bf_op_profile_mixed: invalid trans %d", trans);
+    return BF_EINVAL;
+  }
+  return profile_matvec_mixed(op->op, trans, nrep, ms, bytes, flops, kernels);
+  BF_GUARD_END
+}
+
+int bf_op_mixed_info(bf_op_t op, int64_t* factor_bytes, int64_t* ws_bytes, int64_t* units) {
+  BF_GUARD_BEGIN
+  if (!op) {
+    set_error("bf_op_mixed_info: NULL operator");
+    return BF_EINVAL;
+  }
+  return mixed_info(op->op, factor_bytes, ws_bytes, units);
+  BF_GUARD_END
+}
+
 int bf_op_size(bf_op_t op, int64_t* n_rows, int64_t* n_cols) {
   if (!op) {
     set_error("bf_op_size: NULL operator");

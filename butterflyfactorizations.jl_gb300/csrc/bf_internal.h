@@ -204,6 +204,15 @@ int run_matvec(Operator& op, int trans, int64_t nrhs, const double* x, int64_t l
                int64_t ldy, const double* alpha, const double* beta, int ptr_mode,
                cudaStream_t stream);
 
+// many-RHS tensor-core path (bf_mixed.cu); its state hangs off Operator::mixed
+void mixed_free(void* p);
+int run_matvec_mixed(Operator& op, int trans, int64_t nrhs, const double* x, int64_t ldx,
+                     double* y, int64_t ldy, const double* alpha, const double* beta,
+                     int ptr_mode, cudaStream_t stream);
+int profile_matvec_mixed(Operator& op, int trans, int nrep, double* ms, int64_t* bytes,
+                         double* flops, int64_t* kernels);
+int mixed_info(Operator& op, int64_t* factor_bytes, int64_t* ws_bytes, int64_t* units);
+
 }  // namespace bfg
 
 // opaque C-ABI handles

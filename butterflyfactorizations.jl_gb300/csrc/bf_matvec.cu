@@ -497,6 +497,7 @@ inline int grid_for(int64_t n, int threads) {
 }  // namespace
 
 Operator::~Operator() {
+  if (mixed) mixed_free(mixed);
   if (d_raw) cudaFree(d_raw);
   if (d_A) cudaFree(d_A);
   if (d_tasks) cudaFree(d_tasks);

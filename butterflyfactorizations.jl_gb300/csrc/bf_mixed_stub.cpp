@@ -7,8 +7,3 @@ int surrogate_predict_gpu(const float*, const float*, float*, int64_t, cudaStrea
   return BF_ENOTSUP;
 }
 }  // namespace bfg
-extern "C" int bf_matvec_mixed(bf_op_t, int, int64_t, const double*, int64_t, double*, int64_t,
-                               const double*, const double*, int, void*) {
-  set_error("bf_matvec_mixed: not available in this build");
-  return BF_ENOTSUP;
-}

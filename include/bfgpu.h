@@ -200,9 +200,13 @@ BF_API int bf_matvec_noalloc(bf_op_t op, int trans, int64_t nrhs, const double* 
                              double* y, int64_t ldy, const double* alpha, const double* beta,
                              void* stream);
 
-/* Many-RHS mixed precision: factors in complex FP32, split into BF16 hi/lo and
- * contracted in three tensor-core passes with FP32 accumulation.  Same
- * arguments as bf_matvec; relative error ~1e-5 instead of ~1e-14. */
+/* Many-RHS mixed precision (the column loop of src/Butterflyalgebra/
+ * bfmatrix.jl:10-75 as one dense contraction per level): factors rounded to
+ * complex FP32 and split into BF16 hi/lo, contracted against 128 right-hand
+ * sides at a time in three tensor-core passes with FP32 accumulation.  Same
+ * arguments and semantics as bf_matvec (y <- alpha*op(A)*x + beta*y); relative
+ * error ~1e-5 instead of ~1e-14.  The first call packs the BF16 factors and
+ * allocates a workspace of 1 KB per level slot. */
 BF_API int bf_matvec_mixed(bf_op_t op, int trans, int64_t nrhs, const double* x, int64_t ldx,
                            double* y, int64_t ldy, const double* alpha, const double* beta,
                            int ptr_mode, void* stream);
@@ -253,6 +257,19 @@ BF_API int bf_op_rank_log(bf_op_t op, int64_t* n_rec, double* rec);
  * entry).  Arrays have n_stages entries (bf_op_stats.n_stages). */
 BF_API int bf_op_profile(bf_op_t op, int trans, int32_t nrep, double* ms_per_stage,
                          int64_t* bytes_per_stage, int64_t* kernels_per_matvec);
+
+/* Per-level device time of the mixed path for one chunk of 128 right-hand
+ * sides, with the bytes each level moves (BF16 factor blocks + FP32 slots read
+ * and written) and its useful flops (8 per complex multiply-add and RHS).
+ * No reference counterpart (measurement hook). */
+BF_API int bf_op_profile_mixed(bf_op_t op, int trans, int32_t nrep, double* ms_per_stage,
+                               int64_t* bytes_per_stage, double* flops_per_stage,
+                               int64_t* kernels_per_chunk);
+
+/* Memory of the mixed path: BF16 factor bytes, workspace bytes, work units
+ * (both directions).  Packs the mixed factors if not done yet. */
+BF_API int bf_op_mixed_info(bf_op_t op, int64_t* factor_bytes, int64_t* workspace_bytes,
+                            int64_t* work_units);
 
 /* Shapes of the packed level tasks (stage index, kind 0 = dense / 1 = copy,
  * rows M, columns n), in launch order.  Call with stage == NULL to query
