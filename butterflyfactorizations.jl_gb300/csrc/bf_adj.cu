@@ -36,8 +36,8 @@ __device__ __forceinline__ int rg_of(int M) { return M <= 8 ? 2 : (M <= 32 ? 4 :
 // Partial sums of columns c = c0 + cg + CG*u (u < cpl) over rows
 // [r_begin, r_end) for this lane; summed over the RG lanes of the column group
 // on return (every lane of the group holds the group total).
-template <bool CONJ, int RG>
-__device__ __forceinline__ void adj_pass(const DTask& t, const float4* __restrict__ A,
+template <bool CONJ, int RG, typename FT>
+__device__ __forceinline__ void adj_pass(const DTask& t, const FT* __restrict__ A,
                                          const float4* __restrict__ ws,
                                          const int32_t* __restrict__ rmap, int r_begin, int r_end,
                                          int c0, int cpl, float4 acc[ADJ_CPL]) {
@@ -47,14 +47,14 @@ __device__ __forceinline__ void adj_pass(const DTask& t, const float4* __restric
   const int M = t.M, n = t.n;
 #pragma unroll
   for (int u = 0; u < ADJ_CPL; ++u) acc[u] = make_float4(0.f, 0.f, 0.f, 0.f);
-  const float4* __restrict__ Ab = A + t.a_off;
+  const FT* __restrict__ Ab = A + t.a_off;
   for (int r = r_begin + rg; r < r_end; r += RG) {
     const float4 v = vin(t, rmap, ws, r);
-    float4 a[ADJ_CPL];
+    FT a[ADJ_CPL];
 #pragma unroll
     for (int u = 0; u < ADJ_CPL; ++u) {
       const int c = c0 + cg + CG * u;
-      a[u] = (u < cpl && c < n) ? __ldg(Ab + (size_t)c * M + r) : make_float4(0.f, 0.f, 0.f, 0.f);
+      a[u] = (u < cpl && c < n) ? __ldg(Ab + (size_t)c * M + r) : fac_zero<FT>();
     }
 #pragma unroll
     for (int u = 0; u < ADJ_CPL; ++u) {
@@ -81,8 +81,8 @@ __device__ __forceinline__ void write_out(const DTask& t, const int32_t* __restr
     ws[cmap[c]] = cdf_norm(v);
 }
 
-template <bool CONJ, int RG>
-__device__ void adj_task_warp(const DTask& t, const float4* __restrict__ A,
+template <bool CONJ, int RG, typename FT>
+__device__ void adj_task_warp(const DTask& t, const FT* __restrict__ A,
                               const int32_t* __restrict__ maps, float4* __restrict__ ws,
                               int pass_begin, int pass_step) {
   constexpr int CG = 32 / RG;
@@ -94,7 +94,7 @@ __device__ void adj_task_warp(const DTask& t, const float4* __restrict__ A,
   const int per_pass = CG * cpl;
   float4 acc[ADJ_CPL];
   for (int c0 = pass_begin * per_pass; c0 < t.n; c0 += pass_step * per_pass) {
-    adj_pass<CONJ, RG>(t, A, ws, rmap, 0, t.M, c0, cpl, acc);
+    adj_pass<CONJ, RG, FT>(t, A, ws, rmap, 0, t.M, c0, cpl, acc);
     if (rg == 0) {
 #pragma unroll
       for (int u = 0; u < ADJ_CPL; ++u) {
@@ -106,45 +106,45 @@ __device__ void adj_task_warp(const DTask& t, const float4* __restrict__ A,
 }
 
 // warp per task (small tasks)
-template <bool CONJ>
+template <bool CONJ, typename FT>
 __global__ void __launch_bounds__(256) adj_warp_kernel(const int32_t* __restrict__ tlist,
                                                        int n_tasks,
                                                        const DTask* __restrict__ tasks,
-                                                       const float4* __restrict__ A,
+                                                       const FT* __restrict__ A,
                                                        const int32_t* __restrict__ maps,
                                                        float4* __restrict__ ws) {
   const int ti = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (ti >= n_tasks) return;
   const DTask t = tasks[tlist[ti]];
   switch (rg_of(t.M)) {
-    case 2: adj_task_warp<CONJ, 2>(t, A, maps, ws, 0, 1); break;
-    case 4: adj_task_warp<CONJ, 4>(t, A, maps, ws, 0, 1); break;
-    default: adj_task_warp<CONJ, 8>(t, A, maps, ws, 0, 1); break;
+    case 2: adj_task_warp<CONJ, 2, FT>(t, A, maps, ws, 0, 1); break;
+    case 4: adj_task_warp<CONJ, 4, FT>(t, A, maps, ws, 0, 1); break;
+    default: adj_task_warp<CONJ, 8, FT>(t, A, maps, ws, 0, 1); break;
   }
 }
 
 // CTA per wide task: the 8 warps take column passes round-robin
-template <bool CONJ>
+template <bool CONJ, typename FT>
 __global__ void __launch_bounds__(256) adj_wide_kernel(const int32_t* __restrict__ tlist,
                                                        const DTask* __restrict__ tasks,
-                                                       const float4* __restrict__ A,
+                                                       const FT* __restrict__ A,
                                                        const int32_t* __restrict__ maps,
                                                        float4* __restrict__ ws) {
   const DTask t = tasks[tlist[blockIdx.x]];
   const int w = threadIdx.x >> 5;
   switch (rg_of(t.M)) {
-    case 2: adj_task_warp<CONJ, 2>(t, A, maps, ws, w, 8); break;
-    case 4: adj_task_warp<CONJ, 4>(t, A, maps, ws, w, 8); break;
-    default: adj_task_warp<CONJ, 8>(t, A, maps, ws, w, 8); break;
+    case 2: adj_task_warp<CONJ, 2, FT>(t, A, maps, ws, w, 8); break;
+    case 4: adj_task_warp<CONJ, 4, FT>(t, A, maps, ws, w, 8); break;
+    default: adj_task_warp<CONJ, 8, FT>(t, A, maps, ws, w, 8); break;
   }
 }
 
 // CTA per tall task (M > 32): the 8 warps split the rows; per column pass the
 // warp partials meet in shared memory.
-template <bool CONJ>
+template <bool CONJ, typename FT>
 __global__ void __launch_bounds__(256) adj_tall_kernel(const int32_t* __restrict__ tlist,
                                                        const DTask* __restrict__ tasks,
-                                                       const float4* __restrict__ A,
+                                                       const FT* __restrict__ A,
                                                        const int32_t* __restrict__ maps,
                                                        float4* __restrict__ ws) {
   constexpr int RG = 8, CG = 4;
@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(256) adj_tall_kernel(const int32_t* __restrict
   const int r0 = min(t.M, w * rows_per_warp), r1 = min(t.M, r0 + rows_per_warp);
   float4 acc[ADJ_CPL];
   for (int c0 = 0; c0 < t.n; c0 += per_pass) {
-    adj_pass<CONJ, RG>(t, A, ws, rmap, r0, r1, c0, cpl, acc);
+    adj_pass<CONJ, RG, FT>(t, A, ws, rmap, r0, r1, c0, cpl, acc);
     if (rg == 0) {
 #pragma unroll
       for (int u = 0; u < ADJ_CPL; ++u)
@@ -182,9 +182,10 @@ __global__ void __launch_bounds__(256) adj_tall_kernel(const int32_t* __restrict
 
 }  // namespace
 
-int launch_adj_stage(const Plan& p, int64_t s, bool conj, const int32_t* d_lists,
-                     const DTask* d_tasks, const float4* d_A, const int32_t* d_maps,
-                     float4* d_ws, cudaStream_t st) {
+template <typename FT>
+static int launch_adj_stage_t(const Plan& p, int64_t s, bool conj, const int32_t* d_lists,
+                              const DTask* d_tasks, const FT* d_A, const int32_t* d_maps,
+                              float4* d_ws, cudaStream_t st) {
   auto range = [&](int c, int64_t& b, int64_t& n) {
     b = p.list_begin[c][s];
     n = p.list_begin[c][s + 1] - b;
@@ -195,25 +196,25 @@ int launch_adj_stage(const Plan& p, int64_t s, bool conj, const int32_t* d_lists
   if (n > 0) {
     unsigned g = (unsigned)((n + 7) / 8);
     if (conj)
-      adj_warp_kernel<true><<<g, 256, 0, st>>>(d_lists + b, (int)n, d_tasks, d_A, d_maps, d_ws);
+      adj_warp_kernel<true, FT><<<g, 256, 0, st>>>(d_lists + b, (int)n, d_tasks, d_A, d_maps, d_ws);
     else
-      adj_warp_kernel<false><<<g, 256, 0, st>>>(d_lists + b, (int)n, d_tasks, d_A, d_maps, d_ws);
+      adj_warp_kernel<false, FT><<<g, 256, 0, st>>>(d_lists + b, (int)n, d_tasks, d_A, d_maps, d_ws);
     ++nk;
   }
   range(Plan::L_WIDE, b, n);
   if (n > 0) {
     if (conj)
-      adj_wide_kernel<true><<<(unsigned)n, 256, 0, st>>>(d_lists + b, d_tasks, d_A, d_maps, d_ws);
+      adj_wide_kernel<true, FT><<<(unsigned)n, 256, 0, st>>>(d_lists + b, d_tasks, d_A, d_maps, d_ws);
     else
-      adj_wide_kernel<false><<<(unsigned)n, 256, 0, st>>>(d_lists + b, d_tasks, d_A, d_maps, d_ws);
+      adj_wide_kernel<false, FT><<<(unsigned)n, 256, 0, st>>>(d_lists + b, d_tasks, d_A, d_maps, d_ws);
     ++nk;
   }
   range(Plan::L_ATALL, b, n);
   if (n > 0) {
     if (conj)
-      adj_tall_kernel<true><<<(unsigned)n, 256, 0, st>>>(d_lists + b, d_tasks, d_A, d_maps, d_ws);
+      adj_tall_kernel<true, FT><<<(unsigned)n, 256, 0, st>>>(d_lists + b, d_tasks, d_A, d_maps, d_ws);
     else
-      adj_tall_kernel<false><<<(unsigned)n, 256, 0, st>>>(d_lists + b, d_tasks, d_A, d_maps, d_ws);
+      adj_tall_kernel<false, FT><<<(unsigned)n, 256, 0, st>>>(d_lists + b, d_tasks, d_A, d_maps, d_ws);
     ++nk;
   }
   cudaError_t e = cudaGetLastError();
@@ -222,6 +223,13 @@ int launch_adj_stage(const Plan& p, int64_t s, bool conj, const int32_t* d_lists
     return -1;
   }
   return nk;
+}
+
+int launch_adj_stage(const Plan& p, int64_t s, bool conj, const int32_t* d_lists,
+                     const DTask* d_tasks, const float4* d_A, const float2* d_A2,
+                     const int32_t* d_maps, float4* d_ws, cudaStream_t st) {
+  if (d_A2) return launch_adj_stage_t<float2>(p, s, conj, d_lists, d_tasks, d_A2, d_maps, d_ws, st);
+  return launch_adj_stage_t<float4>(p, s, conj, d_lists, d_tasks, d_A, d_maps, d_ws, st);
 }
 
 }  // namespace bfg

@@ -178,7 +178,7 @@ int bf_import_factors(bf_ctx_t ctx, const bf_factor_desc* d, bf_op_t* out) {
     set_error("bf_import_factors: data is NULL");
     return BF_EINVAL;
   }
-  int s = pack_plan(lg, op.plan);
+  int s = pack_plan(lg, op.plan, (int)sizeof(float4));  // FP64 data: float-float entries
   if (s != BF_OK) {
     delete h;
     return s;
@@ -310,16 +310,19 @@ int bf_op_export_blocks(bf_op_t h, int64_t bf_begin, int64_t bf_end, int64_t* n_
     set_error("bf_op_export_blocks: NULL output array");
     return BF_EINVAL;
   }
-  if (!op.d_raw) {
-    set_error("bf_op_export_blocks: raw factors were released");
+  if (!op.d_A && !op.d_A2) {
+    set_error("bf_op_export_blocks: operator has no factors");
     return BF_ESTATE;
   }
   BF_TRY_CUDA(cudaSetDevice(op.ctx->device));
-  const size_t esz = op.raw_is_double ? 16 : 8;
-  // one bulk copy of the raw store, then a host-side gather per block
-  std::vector<char> raw((size_t)op.raw_entries * esz);
-  if (!raw.empty())
-    BF_TRY_CUDA(cudaMemcpy(raw.data(), op.d_raw, raw.size(), cudaMemcpyDeviceToHost));
+  // one bulk copy of the packed task matrices, then a host-side gather per
+  // block (complex FP32 entries are exact; float-float entries are summed)
+  const bool f32 = op.d_A2 != nullptr;
+  const size_t esz = f32 ? sizeof(float2) : sizeof(float4);
+  std::vector<float> pk((size_t)op.plan.a_entries * esz / sizeof(float));
+  if (!pk.empty())
+    BF_TRY_CUDA(cudaMemcpy(pk.data(), f32 ? (const void*)op.d_A2 : (const void*)op.d_A,
+                           pk.size() * sizeof(float), cudaMemcpyDeviceToHost));
   int64_t off = 0, ob = 0;
   for (size_t b = 0; b < B.size(); ++b) {
     const LBlock& k = B[b];
@@ -336,19 +339,25 @@ int bf_op_export_blocks(bf_op_t h, int64_t bf_begin, int64_t bf_end, int64_t* n_
     data_off[ob] = off;
     ++ob;
     if (k.ident || k.rows * (int64_t)k.cols == 0) continue;
+    const int64_t pko = op.plan.blk_pk_off[b];
+    const size_t pld = (size_t)op.plan.blk_pk_ld[b];
+    if (pko < 0) {
+      set_error("bf_op_export_blocks: block %zu has no packed entries", b);
+      return BF_ESTATE;
+    }
     size_t ncol = (size_t)k.cols, nrow = (size_t)k.rows;
     for (size_t e = 0; e < ncol * nrow; ++e) {
       size_t j = e / nrow, i = e - j * nrow;
-      size_t src = (size_t)k.raw_off + j * (size_t)k.raw_ld + i;
+      size_t src = (size_t)pko + j * pld + i;
       double re, im;
-      if (op.raw_is_double) {
-        const double* p = (const double*)raw.data() + 2 * src;
+      if (f32) {
+        const float* p = pk.data() + 2 * src;
         re = p[0];
         im = p[1];
       } else {
-        const float* p = (const float*)raw.data() + 2 * src;
-        re = p[0];
-        im = p[1];
+        const float* p = pk.data() + 4 * src;
+        re = (double)p[0] + (double)p[1];
+        im = (double)p[2] + (double)p[3];
       }
       if (as_float32) {
         ((float*)data)[2 * (off + e)] = (float)re;

@@ -703,7 +703,8 @@ int build_operator(Context* ctx, const double* obs_xyz, int64_t n_obs, const dou
     Builder b(ctx, to, ts, k, tol, opts, op);
     BF_TRY(b.run(obs_xyz, n_obs, src_xyz, n_src, far_obs, far_src, n_far));
   }
-  BF_TRY(pack_plan(op.logical, op.plan));
+  // the build's factors are complex FP32 values: packed as such (exact)
+  BF_TRY(pack_plan(op.logical, op.plan, op.raw_is_double ? (int)sizeof(float4) : (int)sizeof(float2)));
   BF_TRY(upload_plan(op));
   BF_TRY_CUDA(cudaDeviceSynchronize());
   auto t1 = std::chrono::steady_clock::now();

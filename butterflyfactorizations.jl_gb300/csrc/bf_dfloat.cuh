@@ -61,6 +61,53 @@ __device__ __forceinline__ void cdf_mac_conj(float4& acc, const float4 a, const 
   df_mac(acc.z, acc.w, -a.z, -a.w, x.x, x.y);
 }
 
+// s += a * b with a single float a (a factor stored in complex FP32): the
+// product a*bh is split exactly by the FMA, a*bl joins the low part.
+__device__ __forceinline__ void df_mac1(float& sh, float& sl, float a, float bh, float bl) {
+  float ph = __fmul_rn(a, bh);
+  float pl = __fmaf_rn(a, bh, -ph);
+  pl = __fmaf_rn(a, bl, pl);
+  float s = __fadd_rn(sh, ph);
+  float v = __fsub_rn(s, sh);
+  float e = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, v)), __fsub_rn(ph, v));
+  sh = s;
+  sl = __fadd_rn(sl, __fadd_rn(e, pl));
+}
+
+// acc += a * x, a complex FP32 (re, im)
+__device__ __forceinline__ void cdf_mac(float4& acc, const float2 a, const float4 x) {
+  df_mac1(acc.x, acc.y, a.x, x.x, x.y);
+  df_mac1(acc.x, acc.y, -a.y, x.z, x.w);
+  df_mac1(acc.z, acc.w, a.x, x.z, x.w);
+  df_mac1(acc.z, acc.w, a.y, x.x, x.y);
+}
+
+// acc += conj(a) * x, a complex FP32
+__device__ __forceinline__ void cdf_mac_conj(float4& acc, const float2 a, const float4 x) {
+  df_mac1(acc.x, acc.y, a.x, x.x, x.y);
+  df_mac1(acc.x, acc.y, a.y, x.z, x.w);
+  df_mac1(acc.z, acc.w, a.x, x.z, x.w);
+  df_mac1(acc.z, acc.w, -a.y, x.x, x.y);
+}
+
+// zero factor entry of either storage type
+template <typename FT>
+__device__ __forceinline__ FT fac_zero();
+template <>
+__device__ __forceinline__ float4 fac_zero<float4>() {
+  return make_float4(0.f, 0.f, 0.f, 0.f);
+}
+template <>
+__device__ __forceinline__ float2 fac_zero<float2>() {
+  return make_float2(0.f, 0.f);
+}
+
+// complex FP32 value of a factor entry (float-float entries are rounded)
+__device__ __forceinline__ float2 fac_c32(const float4 a) {
+  return make_float2(a.x + a.y, a.z + a.w);
+}
+__device__ __forceinline__ float2 fac_c32(const float2 a) { return a; }
+
 __device__ __forceinline__ void cdf_add(float4& a, const float4 b) {
   df_add(a.x, a.y, b.x, b.y);
   df_add(a.z, a.w, b.z, b.w);

@@ -7,7 +7,8 @@
 // contiguous workspace range because the x region is stored in leaf order and
 // the level slots in reader order).  Eight consumer warps compute from shared
 // memory in float-float arithmetic and write each output entry once.  The
-// producer keeps up to TMA_NSLOT x 16 KB in flight per CTA regardless of task
+// producer keeps up to NSLOT matrix slots in flight per CTA (4 x 16 KB of
+// float-float entries, 6 x 8 KB of complex FP32 entries) regardless of task
 // boundaries, so the DRAM stream does not stall on per-task set-up.
 //
 // Chunks: a task with M <= TMA_SLOT rows is cut into groups of whole columns
@@ -31,10 +32,22 @@ constexpr int TMA_CT = TMA_CW * 32;           // consumer threads
 constexpr int TMA_THREADS = TMA_CT + 32;      // + one producer warp
 constexpr int TMA_SLOT = 1024;                // complex entries per matrix slot (16 KB)
 constexpr int TMA_XSLOT = 256;                // input entries per slot (4 KB)
-constexpr int TMA_NSLOT = 4;
 constexpr int TMA_FMAX = 256;                 // rows of the per-warp accumulators (mode F)
-constexpr size_t TMA_SMEM = (size_t)TMA_NSLOT * (TMA_SLOT + TMA_XSLOT) * 16 +
-                            (size_t)TMA_CW * TMA_FMAX * 16 + 2 * TMA_NSLOT * 8;
+
+// Matrix slot geometry per factor type.  A bulk copy must start on a 16-byte
+// boundary and move a multiple of 16 bytes: float4 entries always do; for
+// complex FP32 (8-byte) entries a chunk that starts on an odd entry is copied
+// from the entry before it, the slot holds that extra entry in front
+// (`lead`), and the copy is rounded up to an even entry count (the packed
+// factor array has two entries of tail padding for this).
+template <typename FT>
+struct TmaGeom {
+  static constexpr int NSLOT = sizeof(FT) == 8 ? 6 : 4;  // slots in the ring
+  static constexpr int SLOT_E = TMA_SLOT + (sizeof(FT) == 8 ? 2 : 0);
+  static constexpr size_t SMEM = (size_t)NSLOT * SLOT_E * sizeof(FT) +
+                                 (size_t)NSLOT * TMA_XSLOT * 16 +
+                                 (size_t)TMA_CW * TMA_FMAX * 16 + 2 * NSLOT * 8;
+};
 
 struct Chunking {
   int M, n;
@@ -66,19 +79,22 @@ struct Chunking {
   }
 };
 
+template <typename FT>
 __global__ void __launch_bounds__(TMA_THREADS) fwd_tma_kernel(
     const int32_t* __restrict__ tlist, int n_tasks, const DTask* __restrict__ tasks,
-    const float4* __restrict__ A, const int32_t* __restrict__ maps, float4* __restrict__ ws,
+    const FT* __restrict__ A, const int32_t* __restrict__ maps, float4* __restrict__ ws,
     int* __restrict__ err) {
+  constexpr int SLOT_E = TmaGeom<FT>::SLOT_E;
+  constexpr int NSLOT = TmaGeom<FT>::NSLOT;
   extern __shared__ __align__(128) unsigned char smem[];
-  float4* sA = (float4*)smem;                                  // [NSLOT][SLOT]
-  float4* sX = sA + TMA_NSLOT * TMA_SLOT;                      // [NSLOT][XSLOT]
-  float4* sAcc = sX + TMA_NSLOT * TMA_XSLOT;                   // [CW][FMAX]
+  FT* sA = (FT*)smem;                                          // [NSLOT][SLOT_E]
+  float4* sX = (float4*)(sA + NSLOT * SLOT_E);             // [NSLOT][XSLOT]
+  float4* sAcc = sX + NSLOT * TMA_XSLOT;                   // [CW][FMAX]
   uint64_t* bars = (uint64_t*)(sAcc + TMA_CW * TMA_FMAX);      // full[NSLOT], empty[NSLOT]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + TMA_NSLOT);
+  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + NSLOT);
   if (threadIdx.x == 0) {
-    for (int s = 0; s < TMA_NSLOT; ++s) {
+    for (int s = 0; s < NSLOT; ++s) {
       mbar_init(full0 + 8 * s, 1);
       mbar_init(empty0 + 8 * s, TMA_CW);
     }
@@ -91,8 +107,8 @@ __global__ void __launch_bounds__(TMA_THREADS) fwd_tma_kernel(
     if (lane != 0) return;
     int slot = 0;
     uint32_t ph = 0;
-    int issued[TMA_NSLOT];
-    for (int s = 0; s < TMA_NSLOT; ++s) issued[s] = -1;
+    int issued[NSLOT];
+    for (int s = 0; s < NSLOT; ++s) issued[s] = -1;
     bool ok = true;
     for (int ti = blockIdx.x; ti < n_tasks && ok; ti += gridDim.x) {
       const DTask t = tasks[tlist[ti]];
@@ -106,21 +122,25 @@ __global__ void __launch_bounds__(TMA_THREADS) fwd_tma_kernel(
         }
         int c0, cc, r0, rr;
         ch.get(k, c0, cc, r0, rr);
-        const uint32_t abytes = (uint32_t)(cc * rr) * 16u, xbytes = (uint32_t)cc * 16u;
+        const size_t e0 = (size_t)t.a_off + (size_t)c0 * t.M + r0;
+        const int lead = sizeof(FT) == 8 ? (int)(e0 & 1) : 0;
+        int ne = cc * rr + lead;
+        if (sizeof(FT) == 8) ne = (ne + 1) & ~1;
+        const uint32_t abytes = (uint32_t)ne * (uint32_t)sizeof(FT), xbytes = (uint32_t)cc * 16u;
         const uint32_t fb = full0 + 8 * slot;
         fence_proxy_async();
         mbar_arrive_expect_tx(fb, abytes + xbytes);
-        bulk_g2s(smem_u32(sA + slot * TMA_SLOT), A + t.a_off + (size_t)c0 * t.M + r0, abytes, fb);
+        bulk_g2s(smem_u32(sA + slot * SLOT_E), A + (e0 - lead), abytes, fb);
         bulk_g2s(smem_u32(sX + slot * TMA_XSLOT), ws + t.cbase + c0, xbytes, fb);
         issued[slot] = (int)ph;
-        if (++slot == TMA_NSLOT) {
+        if (++slot == NSLOT) {
           slot = 0;
           ph ^= 1u;
         }
       }
     }
     // no copy may still be in flight when the block exits
-    for (int s = 0; s < TMA_NSLOT; ++s)
+    for (int s = 0; s < NSLOT; ++s)
       if (issued[s] >= 0) mbar_wait_drain(full0 + 8 * s, (uint32_t)issued[s], err);
     return;
   }
@@ -155,7 +175,9 @@ __global__ void __launch_bounds__(TMA_THREADS) fwd_tma_kernel(
       dead = __any_sync(0xffffffffu, !got);
       int c0, cc, r0, rr;
       ch.get(k, c0, cc, r0, rr);
-      const float4* __restrict__ a = sA + slot * TMA_SLOT;
+      const int lead =
+          sizeof(FT) == 8 ? (int)(((size_t)t.a_off + (size_t)c0 * M + r0) & 1) : 0;
+      const FT* __restrict__ a = sA + slot * SLOT_E + lead;
       const float4* __restrict__ xv = sX + slot * TMA_XSLOT;
       if (dead) {
         // skip the data; still release the slot below
@@ -168,10 +190,15 @@ __global__ void __launch_bounds__(TMA_THREADS) fwd_tma_kernel(
         const int e0 = warp * per, e1 = min(E, e0 + per);
         int e = e0 + lane;
         int col = e / M, row = e - col * M;
-        for (; e < e1; e += 32) {
-          float4 s = accw[row];
-          cdf_mac(s, a[e], xv[col]);
-          accw[row] = s;
+        // warp-uniform trip count; the warp barrier orders read-modify-writes
+        // of one row by different lanes in consecutive steps
+        for (; e - lane < e1; e += 32) {
+          if (e < e1) {
+            float4 s = accw[row];
+            cdf_mac(s, a[e], xv[col]);
+            accw[row] = s;
+          }
+          __syncwarp();
           row += 32;
           if (row >= M) {
             row -= M;
@@ -196,7 +223,7 @@ __global__ void __launch_bounds__(TMA_THREADS) fwd_tma_kernel(
       }
       __syncwarp();
       if (lane == 0) mbar_arrive(empty0 + 8 * slot);
-      if (++slot == TMA_NSLOT) {
+      if (++slot == NSLOT) {
         slot = 0;
         ph ^= 1u;
       }
@@ -239,20 +266,27 @@ __global__ void __launch_bounds__(TMA_THREADS) fwd_tma_kernel(
 
 }  // namespace
 
-int launch_fwd_tma(const int32_t* d_tlist, int n_tasks, const DTask* d_tasks, const float4* d_A,
-                   const int32_t* d_maps, float4* d_ws, int* d_err, int n_sm, cudaStream_t st) {
-  if (n_tasks <= 0) return BF_OK;
-  static bool attr = false;
-  if (!attr) {
-    BF_TRY_CUDA(cudaFuncSetAttribute(fwd_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)TMA_SMEM));
-    attr = true;
-  }
+template <typename FT>
+static int launch_fwd_tma_t(const int32_t* d_tlist, int n_tasks, const DTask* d_tasks,
+                            const FT* d_A, const int32_t* d_maps, float4* d_ws, int* d_err,
+                            int n_sm, cudaStream_t st) {
+  constexpr size_t smem = TmaGeom<FT>::SMEM;
+  BF_TRY_CUDA(cudaFuncSetAttribute(fwd_tma_kernel<FT>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int grid = std::min(n_tasks, 2 * n_sm);
-  fwd_tma_kernel<<<grid, TMA_THREADS, TMA_SMEM, st>>>(d_tlist, n_tasks, d_tasks, d_A, d_maps,
+  fwd_tma_kernel<FT><<<grid, TMA_THREADS, smem, st>>>(d_tlist, n_tasks, d_tasks, d_A, d_maps,
                                                         d_ws, d_err);
   BF_TRY_CUDA(cudaGetLastError());
   return BF_OK;
+}
+
+int launch_fwd_tma(const int32_t* d_tlist, int n_tasks, const DTask* d_tasks, const float4* d_A,
+                   const float2* d_A2, const int32_t* d_maps, float4* d_ws, int* d_err, int n_sm,
+                   cudaStream_t st) {
+  if (n_tasks <= 0) return BF_OK;
+  if (d_A2)
+    return launch_fwd_tma_t<float2>(d_tlist, n_tasks, d_tasks, d_A2, d_maps, d_ws, d_err, n_sm, st);
+  return launch_fwd_tma_t<float4>(d_tlist, n_tasks, d_tasks, d_A, d_maps, d_ws, d_err, n_sm, st);
 }
 
 }  // namespace bfg

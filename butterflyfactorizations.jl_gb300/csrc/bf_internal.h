@@ -134,7 +134,12 @@ struct Plan {
   std::vector<uint8_t> stage_tma;
   std::vector<int32_t> maps;
   int64_t a_entries = 0;
+  int fac_bytes = 16;  // bytes per packed factor entry: 16 float-float, 8 complex FP32
   std::vector<DSeg> segs;
+  // per logical block: offset and leading dimension of its entries inside the
+  // packed task matrices (-1: identity / empty), used by bf_op_export_blocks
+  std::vector<int64_t> blk_pk_off;
+  std::vector<int32_t> blk_pk_ld;
   bool yg_covered = false, xg_covered = false;
   int64_t alg_bytes_fwd = 0;
   int64_t block_entries = 0;
@@ -143,7 +148,7 @@ struct Plan {
   int64_t n_stages() const { return (int64_t)stage_begin.size() - 1; }
 };
 
-int pack_plan(const Logical& lg, Plan& plan);
+int pack_plan(const Logical& lg, Plan& plan, int fac_bytes);
 
 // ---------------------------------------------------------------- device-side
 struct Context {
@@ -157,10 +162,13 @@ struct Operator {
   Plan plan;
   Logical logical;
   int raw_is_double = 1;
-  void* d_raw = nullptr;  // raw logical block data (double2 or float2)
+  void* d_raw = nullptr;  // raw logical block data (double2 or float2); freed after packing
   int64_t raw_entries = 0;
-  // plain (FP64-accurate) operator: float-float factors
+  // plain (FP64-accurate) operator: packed task matrices, float-float entries
+  // (d_A, from FP64 factors) or complex FP32 entries (d_A2, from the GPU
+  // build, whose factors are FP32 values); exactly one is set
   float4* d_A = nullptr;
+  float2* d_A2 = nullptr;
   DTask* d_tasks = nullptr;
   int32_t* d_maps = nullptr;
   float4* d_ws = nullptr;
@@ -194,12 +202,15 @@ int build_operator(Context* ctx, const double* obs_xyz, int64_t n_obs, const dou
                    const bf_build_opts& opts, Operator& op);
 int profile_matvec(Operator& op, int trans, int nrep, double* ms, int64_t* bytes,
                    int64_t* kernels);
+// The launchers take both factor pointers; the non-null one selects the
+// float-float (d_A) or complex FP32 (d_A2) instantiation.
 int launch_fwd_tma(const int32_t* d_tlist, int n_tasks, const DTask* d_tasks, const float4* d_A,
-                   const int32_t* d_maps, float4* d_ws, int* d_err, int n_sm, cudaStream_t st);
+                   const float2* d_A2, const int32_t* d_maps, float4* d_ws, int* d_err, int n_sm,
+                   cudaStream_t st);
 // adjoint (conj) / transpose launches of level s; returns the kernel count or -1
 int launch_adj_stage(const Plan& p, int64_t s, bool conj, const int32_t* d_lists,
-                     const DTask* d_tasks, const float4* d_A, const int32_t* d_maps,
-                     float4* d_ws, cudaStream_t st);
+                     const DTask* d_tasks, const float4* d_A, const float2* d_A2,
+                     const int32_t* d_maps, float4* d_ws, cudaStream_t st);
 int run_matvec(Operator& op, int trans, int64_t nrhs, const double* x, int64_t ldx, double* y,
                int64_t ldy, const double* alpha, const double* beta, int ptr_mode,
                cudaStream_t stream);

@@ -22,163 +22,29 @@
 namespace bfg {
 namespace {
 
-constexpr int NT = 256;   // threads per task CTA
-constexpr int CH = 2048;  // staged matrix entries per chunk (32 KB)
-constexpr int XC = 512;   // staged input entries per chunk
-constexpr int RPT = 4;    // rows per thread per row tile (forward)
-
-__device__ __forceinline__ int pow2_threads(int m) {
-  return m <= 32 ? 32 : (m <= 64 ? 64 : (m <= 128 ? 128 : 256));
-}
-
-// forward: ws[rmap[i]] = sum_j A[i,j] ws[cmap[j]]
-__global__ void __launch_bounds__(NT) stage_fwd_kernel(const DTask* __restrict__ tasks,
-                                                       const float4* __restrict__ A,
-                                                       const int32_t* __restrict__ maps,
-                                                       float4* __restrict__ ws) {
-  __shared__ float4 sA[CH];
-  __shared__ float4 sx[XC];
-  const DTask t = tasks[blockIdx.x];
-  const int32_t* __restrict__ rmap = maps + t.rmap_off;
-  const int32_t* __restrict__ cmap = maps + t.cmap_off;
-  const int tid = threadIdx.x;
-  if (t.kind == TASK_COPY) {
-    for (int i = tid; i < t.M; i += NT) ws[rmap[i]] = ws[cmap[i]];
-    return;
-  }
-  const int M = t.M, n = t.n;
-  const float4* __restrict__ Ag = A + t.a_off;
-  const int P = pow2_threads(M);
-  const int S = NT / P;
-  const int p = tid % P, s = tid / P;
-  for (int r0 = 0; r0 < M; r0 += P * RPT) {
-    const int TR = min(M - r0, P * RPT);
-    int TC = max(1, CH / TR);
-    TC = min(TC, XC);
-    float4 acc[RPT];
-#pragma unroll
-    for (int k = 0; k < RPT; ++k) acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int c0 = 0; c0 < n; c0 += TC) {
-      const int tc = min(TC, n - c0);
-      const float4* __restrict__ src = Ag + (size_t)c0 * M + r0;
-      if (TR == M) {
-        const int tot = tc * TR;  // contiguous columns
-        for (int e = tid; e < tot; e += NT) sA[e] = __ldg(src + e);
-      } else {
-        for (int e = tid; e < tc * TR; e += NT) {
-          int jj = e / TR, ii = e - jj * TR;
-          sA[e] = __ldg(src + (size_t)jj * M + ii);
-        }
-      }
-      for (int e = tid; e < tc; e += NT) sx[e] = ws[cmap[c0 + e]];
-      __syncthreads();
-      for (int jj = s; jj < tc; jj += S) {
-        const float4 xv = sx[jj];
-#pragma unroll
-        for (int k = 0; k < RPT; ++k) {
-          int ii = p + k * P;
-          if (ii < TR) cdf_mac(acc[k], sA[jj * TR + ii], xv);
-        }
-      }
-      __syncthreads();
-    }
-    // reduce the S column splits and write
-#pragma unroll
-    for (int k = 0; k < RPT; ++k) {
-      int ii = p + k * P;
-      if (S > 1) {
-        sA[tid] = acc[k];
-        __syncthreads();
-        if (s == 0 && ii < TR) {
-          float4 v = sA[p];
-          for (int q = 1; q < S; ++q) cdf_add(v, sA[p + q * P]);
-          ws[rmap[r0 + ii]] = cdf_norm(v);
-        }
-        __syncthreads();
-      } else if (ii < TR) {
-        ws[rmap[r0 + ii]] = cdf_norm(acc[k]);
-      }
-    }
-  }
-}
-
-// adjoint (CONJ) or transpose: ws[cmap[j]] = sum_i op(A[i,j]) ws[rmap[i]]
-template <bool CONJ>
-__global__ void __launch_bounds__(NT) stage_adj_kernel(const DTask* __restrict__ tasks,
-                                                       const float4* __restrict__ A,
-                                                       const int32_t* __restrict__ maps,
-                                                       float4* __restrict__ ws) {
-  __shared__ float4 sA[CH + NT];
-  __shared__ float4 sv[CH / 32];
-  const DTask t = tasks[blockIdx.x];
-  const int32_t* __restrict__ rmap = maps + t.rmap_off;
-  const int32_t* __restrict__ cmap = maps + t.cmap_off;
-  const int tid = threadIdx.x;
-  if (t.kind == TASK_COPY) {
-    for (int i = tid; i < t.M; i += NT) ws[cmap[i]] = ws[rmap[i]];
-    return;
-  }
-  const int M = t.M, n = t.n;
-  const float4* __restrict__ Ag = A + t.a_off;
-  const int Pc = pow2_threads(n);
-  const int S = NT / Pc;
-  const int q = tid % Pc, s = tid / Pc;
-  const int TRmax = CH / Pc;  // >= 8, power of two
-  const int LDS = TRmax + 1;  // odd stride: conflict-free column reads
-  for (int c0 = 0; c0 < n; c0 += Pc) {
-    const int tc = min(Pc, n - c0);
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int r0 = 0; r0 < M; r0 += TRmax) {
-      const int tr = min(TRmax, M - r0);
-      const float4* __restrict__ src = Ag + (size_t)c0 * M + r0;
-      for (int e = tid; e < tc * tr; e += NT) {
-        int jj = e / tr, ii = e - jj * tr;
-        sA[jj * LDS + ii] = __ldg(src + (size_t)jj * M + ii);
-      }
-      for (int e = tid; e < tr; e += NT) sv[e] = ws[rmap[r0 + e]];
-      __syncthreads();
-      if (q < tc) {
-        for (int ii = s; ii < tr; ii += S) {
-          const float4 a = sA[q * LDS + ii];
-          if (CONJ)
-            cdf_mac_conj(acc, a, sv[ii]);
-          else
-            cdf_mac(acc, a, sv[ii]);
-        }
-      }
-      __syncthreads();
-    }
-    if (S > 1) {
-      sA[tid] = acc;
-      __syncthreads();
-      if (s == 0 && q < tc) {
-        float4 v = sA[q];
-        for (int r = 1; r < S; ++r) cdf_add(v, sA[q + r * Pc]);
-        ws[cmap[c0 + q]] = cdf_norm(v);
-      }
-      __syncthreads();
-    } else if (q < tc) {
-      ws[cmap[c0 + q]] = cdf_norm(acc);
-    }
-  }
-}
-
-// raw logical blocks -> packed float-float task matrices
-template <typename SrcT>
+// raw logical blocks -> packed task matrices: complex FP64 raw data becomes
+// float-float entries (float4), complex FP32 raw data (the GPU build's output)
+// is kept as complex FP32 (float2), which is exact and half the bytes.
+template <typename SrcT, typename FT>
 __global__ void repack_kernel(const DSeg* __restrict__ segs, const SrcT* __restrict__ raw,
-                              float4* __restrict__ A) {
+                              FT* __restrict__ A) {
   const DSeg g = segs[blockIdx.x];
   if (g.kind == 1) {
-    for (int i = threadIdx.x; i < g.rows; i += blockDim.x)
-      A[g.dst_off + (size_t)i * g.dst_ld + i] = make_float4(1.f, 0.f, 0.f, 0.f);
+    for (int i = threadIdx.x; i < g.rows; i += blockDim.x) {
+      FT one = fac_zero<FT>();
+      one.x = 1.f;
+      A[g.dst_off + (size_t)i * g.dst_ld + i] = one;
+    }
     return;
   }
   const long long tot = (long long)g.rows * g.cols;
   for (long long e = threadIdx.x; e < tot; e += blockDim.x) {
     int j = (int)(e / g.rows), i = (int)(e - (long long)j * g.rows);
     SrcT v = raw[g.src_off + (size_t)j * g.src_ld + i];
-    float4 o;
-    if constexpr (sizeof(SrcT) == 16) {
+    FT o;
+    if constexpr (sizeof(FT) == 8) {
+      o = make_float2((float)v.x, (float)v.y);
+    } else if constexpr (sizeof(SrcT) == 16) {
       float2 re = df_split(v.x), im = df_split(v.y);
       o = make_float4(re.x, re.y, im.x, im.y);
     } else {
@@ -237,9 +103,10 @@ constexpr int FW_WARPS = 8;
 constexpr int FW_XB = 256;  // staged input entries per warp per pass
 constexpr int TALL_RPL = TALL_ROWS / 32;  // rows per lane in the tall kernel
 
+template <typename FT>
 __global__ void __launch_bounds__(FW_WARPS * 32) fwd_tall_kernel(
     const int2* __restrict__ items, int n_items, const DTask* __restrict__ tasks,
-    const float4* __restrict__ A, const int32_t* __restrict__ maps, float4* __restrict__ ws) {
+    const FT* __restrict__ A, const int32_t* __restrict__ maps, float4* __restrict__ ws) {
   __shared__ float4 xs[FW_WARPS][FW_XB];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int item = blockIdx.x * FW_WARPS + warp;
@@ -272,16 +139,18 @@ __global__ void __launch_bounds__(FW_WARPS * 32) fwd_tall_kernel(
       for (int j = lane; j < nb; j += 32) xw[j] = t.cbase >= 0 ? ws[t.cbase + cb + j] : ws[cmap[cb + j]];
       __syncwarp();
     }
-    const float4* __restrict__ ap = A + t.a_off + (size_t)cb * M + r0 + lane;
+    const FT* __restrict__ ap = A + t.a_off + (size_t)cb * M + r0 + lane;
     int j = 0;
-    constexpr int CPI = 8 / TALL_RPL;  // columns per iteration: eight loads in flight
+    // columns per iteration: 128 bytes of loads in flight per lane (eight
+    // float-float or sixteen complex FP32 entries)
+    constexpr int CPI = (sizeof(FT) == 8 ? 16 : 8) / TALL_RPL;
     for (; j + CPI - 1 < nb; j += CPI) {
-      float4 a[CPI][TALL_RPL];
+      FT a[CPI][TALL_RPL];
 #pragma unroll
       for (int c = 0; c < CPI; ++c)
 #pragma unroll
         for (int q = 0; q < TALL_RPL; ++q)
-          a[c][q] = act[q] ? __ldg(ap + (size_t)c * M + 32 * q) : make_float4(0.f, 0.f, 0.f, 0.f);
+          a[c][q] = act[q] ? __ldg(ap + (size_t)c * M + 32 * q) : fac_zero<FT>();
 #pragma unroll
       for (int c = 0; c < CPI; ++c) {
         const float4 xc = xw[j + c];
@@ -315,9 +184,10 @@ __global__ void __launch_bounds__(FW_WARPS * 32) fwd_tall_kernel(
 // column-major M x n matrix.  With M > 32 the 32 entries of one warp load
 // belong to 32 distinct rows, so each lane adds its product into a per-row
 // accumulator in warp-private shared memory without conflicts.
+template <typename FT>
 __global__ void __launch_bounds__(FW_WARPS * 32) fwd_flat_kernel(
     const int32_t* __restrict__ tlist, int n_tasks, const DTask* __restrict__ tasks,
-    const float4* __restrict__ A, const int32_t* __restrict__ maps, float4* __restrict__ ws) {
+    const FT* __restrict__ A, const int32_t* __restrict__ maps, float4* __restrict__ ws) {
   __shared__ float4 xs[FW_WARPS][FLAT_NMAX];
   __shared__ float4 as[FW_WARPS][FLAT_MMAX];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -333,18 +203,22 @@ __global__ void __launch_bounds__(FW_WARPS * 32) fwd_flat_kernel(
   for (int i = lane; i < M; i += 32) aw[i] = make_float4(0.f, 0.f, 0.f, 0.f);
   __syncwarp();
   const long long tot = (long long)M * n;
-  const float4* __restrict__ ap = A + t.a_off;
+  const FT* __restrict__ ap = A + t.a_off;
   int row = lane, col = 0;  // entry lane: row lane of column 0 (M > 32)
   long long e = lane;
-  for (; e + 96 < tot; e += 128) {  // four loads in flight
-    const float4 a0 = __ldg(ap + e), a1 = __ldg(ap + e + 32), a2 = __ldg(ap + e + 64),
-                 a3 = __ldg(ap + e + 96);
-    const float4 v[4] = {a0, a1, a2, a3};
+  constexpr int LU = sizeof(FT) == 8 ? 8 : 4;  // loads in flight: 64 bytes per lane
+  for (; e - lane + 32 * LU <= tot; e += 32 * LU) {  // warp-uniform: whole warp steps fit
+    FT v[LU];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < LU; ++u) v[u] = __ldg(ap + e + 32 * u);
+    // lane a at step u+1 can hit the row that lane a-(M-32) updates at step
+    // u: the warp barrier orders the two read-modify-writes
+#pragma unroll
+    for (int u = 0; u < LU; ++u) {
       float4 s = aw[row];
       cdf_mac(s, v[u], xw[col]);
       aw[row] = s;
+      __syncwarp();
       row += 32;
       if (row >= M) {
         row -= M;
@@ -352,10 +226,13 @@ __global__ void __launch_bounds__(FW_WARPS * 32) fwd_flat_kernel(
       }
     }
   }
-  for (; e < tot; e += 32) {
-    float4 s = aw[row];
-    cdf_mac(s, __ldg(ap + e), xw[col]);
-    aw[row] = s;
+  for (; e - lane < tot; e += 32) {  // warp-uniform trip count
+    if (e < tot) {
+      float4 s = aw[row];
+      cdf_mac(s, __ldg(ap + e), xw[col]);
+      aw[row] = s;
+    }
+    __syncwarp();
     row += 32;
     if (row >= M) {
       row -= M;
@@ -368,9 +245,10 @@ __global__ void __launch_bounds__(FW_WARPS * 32) fwd_flat_kernel(
 
 // M <= 32: G = 32/M lane groups walk interleaved columns (one warp load reads
 // G*M contiguous entries); the groups meet in shared memory at the end.
+template <typename FT>
 __global__ void __launch_bounds__(FW_WARPS * 32) fwd_small_kernel(
     const int32_t* __restrict__ tlist, int n_tasks, const DTask* __restrict__ tasks,
-    const float4* __restrict__ A, const int32_t* __restrict__ maps, float4* __restrict__ ws) {
+    const FT* __restrict__ A, const int32_t* __restrict__ maps, float4* __restrict__ ws) {
   __shared__ float4 xs[FW_WARPS][FW_XB];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ti = blockIdx.x * FW_WARPS + warp;
@@ -390,16 +268,16 @@ __global__ void __launch_bounds__(FW_WARPS * 32) fwd_small_kernel(
     __syncwarp();
     if (active) {
       const size_t step = (size_t)G * M;
-      const float4* __restrict__ ap = A + t.a_off + (size_t)(cb + g) * M + i;
+      const FT* __restrict__ ap = A + t.a_off + (size_t)(cb + g) * M + i;
       int j = g;
-      for (; j + 3 * G < nb; j += 4 * G) {
-        const float4 a0 = __ldg(ap), a1 = __ldg(ap + step), a2 = __ldg(ap + 2 * step),
-                     a3 = __ldg(ap + 3 * step);
-        cdf_mac(acc, a0, xw[j]);
-        cdf_mac(acc, a1, xw[j + G]);
-        cdf_mac(acc, a2, xw[j + 2 * G]);
-        cdf_mac(acc, a3, xw[j + 3 * G]);
-        ap += 4 * step;
+      constexpr int LU = sizeof(FT) == 8 ? 8 : 4;  // loads in flight
+      for (; j + (LU - 1) * G < nb; j += LU * G) {
+        FT a[LU];
+#pragma unroll
+        for (int u = 0; u < LU; ++u) a[u] = __ldg(ap + u * step);
+#pragma unroll
+        for (int u = 0; u < LU; ++u) cdf_mac(acc, a[u], xw[j + u * G]);
+        ap += LU * step;
       }
       for (; j < nb; j += G) {
         cdf_mac(acc, __ldg(ap), xw[j]);
@@ -441,9 +319,10 @@ __global__ void copy_kernel(const int32_t* __restrict__ tlist, int n_tasks,
 // Forward for short wide tasks (M <= 32, many columns: the P stage).  One CTA
 // per task; warps split the columns, lane groups (G = 32/M per warp) read G*M
 // contiguous entries per load; partial row sums meet in shared memory.
+template <typename FT>
 __global__ void __launch_bounds__(256) fwd_wide_kernel(const int32_t* __restrict__ tlist,
                                                        const DTask* __restrict__ tasks,
-                                                       const float4* __restrict__ A,
+                                                       const FT* __restrict__ A,
                                                        const int32_t* __restrict__ maps,
                                                        float4* __restrict__ ws) {
   __shared__ float4 red[8][32];
@@ -460,17 +339,18 @@ __global__ void __launch_bounds__(256) fwd_wide_kernel(const int32_t* __restrict
     const int cstep = 8 * G;
     const size_t step = (size_t)cstep * M;
     int j = warp * G + g;
-    const float4* __restrict__ ap = A + t.a_off + (size_t)j * M + i;
-    for (; j + 3 * cstep < n; j += 4 * cstep) {
-      const float4 a0 = __ldg(ap), a1 = __ldg(ap + step), a2 = __ldg(ap + 2 * step),
-                   a3 = __ldg(ap + 3 * step);
-      const float4 x0 = ws[cmap[j]], x1 = ws[cmap[j + cstep]], x2 = ws[cmap[j + 2 * cstep]],
-                   x3 = ws[cmap[j + 3 * cstep]];
-      cdf_mac(acc, a0, x0);
-      cdf_mac(acc, a1, x1);
-      cdf_mac(acc, a2, x2);
-      cdf_mac(acc, a3, x3);
-      ap += 4 * step;
+    const FT* __restrict__ ap = A + t.a_off + (size_t)j * M + i;
+    constexpr int LU = sizeof(FT) == 8 ? 8 : 4;  // loads in flight
+    for (; j + (LU - 1) * cstep < n; j += LU * cstep) {
+      FT a[LU];
+      float4 x[LU];
+#pragma unroll
+      for (int u = 0; u < LU; ++u) a[u] = __ldg(ap + u * step);
+#pragma unroll
+      for (int u = 0; u < LU; ++u) x[u] = ws[cmap[j + u * cstep]];
+#pragma unroll
+      for (int u = 0; u < LU; ++u) cdf_mac(acc, a[u], x[u]);
+      ap += LU * step;
     }
     for (; j < n; j += cstep) {
       cdf_mac(acc, __ldg(ap), ws[cmap[j]]);
@@ -500,6 +380,7 @@ Operator::~Operator() {
   if (mixed) mixed_free(mixed);
   if (d_raw) cudaFree(d_raw);
   if (d_A) cudaFree(d_A);
+  if (d_A2) cudaFree(d_A2);
   if (d_tasks) cudaFree(d_tasks);
   if (d_maps) cudaFree(d_maps);
   if (d_ws) cudaFree(d_ws);
@@ -516,13 +397,27 @@ int upload_plan(Operator& op) {
   Plan& p = op.plan;
   BF_TRY_CUDA(cudaSetDevice(op.ctx->device));
   if (!op.stream) BF_TRY_CUDA(cudaStreamCreateWithFlags(&op.stream, cudaStreamNonBlocking));
-  size_t abytes = (size_t)std::max<int64_t>(p.a_entries, 1) * sizeof(float4);
-  if (cudaMalloc(&op.d_A, abytes) != cudaSuccess) {
+  // FP64 factors -> float-float (16 B), complex FP32 factors (GPU build) stay
+  // complex FP32 (8 B); two entries of tail padding serve the 16-byte rounding
+  // of the bulk copies (bf_fwd_tma.cu)
+  const bool f32 = !op.raw_is_double;
+  const size_t esz = f32 ? sizeof(float2) : sizeof(float4);
+  if ((size_t)p.fac_bytes != esz) {
+    set_error("upload: plan packed for %d-byte factors, data has %zu", p.fac_bytes, esz);
+    return BF_ESTATE;
+  }
+  size_t abytes = (size_t)(std::max<int64_t>(p.a_entries, 1) + 2) * esz;
+  void* dA = nullptr;
+  if (cudaMalloc(&dA, abytes) != cudaSuccess) {
     cudaGetLastError();
     set_error("upload: cannot allocate %zu bytes of factors", abytes);
     return BF_ENOMEM;
   }
-  BF_TRY_CUDA(cudaMemsetAsync(op.d_A, 0, abytes, op.stream));
+  if (f32)
+    op.d_A2 = (float2*)dA;
+  else
+    op.d_A = (float4*)dA;
+  BF_TRY_CUDA(cudaMemsetAsync(dA, 0, abytes, op.stream));
   if (!p.segs.empty()) {
     DSeg* d_segs = nullptr;
     BF_TRY_CUDA(cudaMalloc(&d_segs, p.segs.size() * sizeof(DSeg)));
@@ -530,14 +425,19 @@ int upload_plan(Operator& op) {
                                 cudaMemcpyHostToDevice, op.stream));
     // gridDim.x limit is 2^31-1; segment counts stay far below
     if (op.raw_is_double)
-      repack_kernel<double2><<<(unsigned)p.segs.size(), 128, 0, op.stream>>>(
+      repack_kernel<double2, float4><<<(unsigned)p.segs.size(), 128, 0, op.stream>>>(
           d_segs, (const double2*)op.d_raw, op.d_A);
     else
-      repack_kernel<float2><<<(unsigned)p.segs.size(), 128, 0, op.stream>>>(
-          d_segs, (const float2*)op.d_raw, op.d_A);
+      repack_kernel<float2, float2><<<(unsigned)p.segs.size(), 128, 0, op.stream>>>(
+          d_segs, (const float2*)op.d_raw, op.d_A2);
     BF_TRY_CUDA(cudaGetLastError());
     BF_TRY_CUDA(cudaStreamSynchronize(op.stream));
     cudaFree(d_segs);
+  }
+  // the packed matrices are the only factor copy from here on (export reads them)
+  if (op.d_raw) {
+    cudaFree(op.d_raw);
+    op.d_raw = nullptr;
   }
   BF_TRY_CUDA(cudaMalloc(&op.d_tasks, std::max<size_t>(1, p.tasks.size()) * sizeof(DTask)));
   BF_TRY_CUDA(cudaMemcpy(op.d_tasks, p.tasks.data(), p.tasks.size() * sizeof(DTask),
@@ -574,7 +474,7 @@ int upload_plan(Operator& op) {
   op.stats.n_stages = p.n_stages();
   op.stats.n_tasks = (int64_t)p.tasks.size();
   op.stats.factor_entries = p.a_entries;
-  op.stats.factor_bytes = p.a_entries * (int64_t)sizeof(float4);
+  op.stats.factor_bytes = p.a_entries * (int64_t)esz;
   op.stats.workspace_entries = p.ws_entries;
   op.stats.map_entries = (int64_t)p.maps.size();
   op.stats.alg_bytes_fwd = p.alg_bytes_fwd;
@@ -582,60 +482,67 @@ int upload_plan(Operator& op) {
   return BF_OK;
 }
 
+// Forward launches of level s with factor entries of type FT.
+template <typename FT>
+static int launch_fwd_stage(Operator& op, int64_t s, cudaStream_t st, float4* ws, const FT* A) {
+  const Plan& p = op.plan;
+  int nk = 0;
+  auto range = [&](int c, int64_t& b, int64_t& n) {
+    b = p.list_begin[c][s];
+    n = p.list_begin[c][s + 1] - b;
+  };
+  int64_t b, n;
+  const unsigned WT = FW_WARPS * 32;
+  // short wide tasks (the P stage) stream through the bulk-copy pipeline; the
+  // many small R-level tasks and the tall Q tasks run the direct-load kernels
+  const bool tma_wide = p.stage_tma[s] && op.fwd_kernel == 0;
+  range(Plan::L_TALL, b, n);
+  if (n > 0) {
+    int64_t items = n / 2;
+    fwd_tall_kernel<FT><<<(unsigned)((items + FW_WARPS - 1) / FW_WARPS), WT, 0, st>>>(
+        (const int2*)(op.d_lists + b), (int)items, op.d_tasks, A, op.d_maps, ws);
+    ++nk;
+  }
+  range(Plan::L_FLAT, b, n);
+  if (n > 0) {
+    fwd_flat_kernel<FT><<<(unsigned)((n + FW_WARPS - 1) / FW_WARPS), WT, 0, st>>>(
+        op.d_lists + b, (int)n, op.d_tasks, A, op.d_maps, ws);
+    ++nk;
+  }
+  range(Plan::L_SMALL, b, n);
+  if (n > 0) {
+    fwd_small_kernel<FT><<<(unsigned)((n + FW_WARPS - 1) / FW_WARPS), WT, 0, st>>>(
+        op.d_lists + b, (int)n, op.d_tasks, A, op.d_maps, ws);
+    ++nk;
+  }
+  range(Plan::L_WIDE, b, n);
+  if (n > 0 && tma_wide) {
+    BF_TRY(launch_fwd_tma(op.d_lists + b, (int)n, op.d_tasks, op.d_A, op.d_A2, op.d_maps, ws,
+                          op.d_err, op.ctx->prop.multiProcessorCount, st));
+    ++nk;
+  } else if (n > 0) {
+    fwd_wide_kernel<FT><<<(unsigned)n, 256, 0, st>>>(op.d_lists + b, op.d_tasks, A, op.d_maps, ws);
+    ++nk;
+  }
+  range(Plan::L_COPY, b, n);
+  if (n > 0) {
+    copy_kernel<<<(unsigned)((n + 7) / 8), 256, 0, st>>>(op.d_lists + b, (int)n, op.d_tasks,
+                                                         op.d_maps, ws, 0);
+    ++nk;
+  }
+  return nk;
+}
+
 // Launches of level s for direction trans; returns the number of kernels.
 static int launch_stage(Operator& op, int64_t s, int trans, cudaStream_t st, float4* ws) {
   const Plan& p = op.plan;
   int nk = 0;
-  if (trans == BF_OP_N) {
-    auto range = [&](int c, int64_t& b, int64_t& n) {
-      b = p.list_begin[c][s];
-      n = p.list_begin[c][s + 1] - b;
-    };
-    int64_t b, n;
-    const unsigned WT = FW_WARPS * 32;
-    // short wide tasks (the P stage) stream through the bulk-copy pipeline; the
-    // many small R-level tasks and the tall Q tasks run the direct-load kernels
-    const bool tma_wide = p.stage_tma[s] && op.fwd_kernel == 0;
-    range(Plan::L_TALL, b, n);
-    if (n > 0) {
-      int64_t items = n / 2;
-      fwd_tall_kernel<<<(unsigned)((items + FW_WARPS - 1) / FW_WARPS), WT, 0, st>>>(
-          (const int2*)(op.d_lists + b), (int)items, op.d_tasks, op.d_A, op.d_maps, ws);
-      ++nk;
-    }
-    range(Plan::L_FLAT, b, n);
-    if (n > 0) {
-      fwd_flat_kernel<<<(unsigned)((n + FW_WARPS - 1) / FW_WARPS), WT, 0, st>>>(
-          op.d_lists + b, (int)n, op.d_tasks, op.d_A, op.d_maps, ws);
-      ++nk;
-    }
-    range(Plan::L_SMALL, b, n);
-    if (n > 0) {
-      fwd_small_kernel<<<(unsigned)((n + FW_WARPS - 1) / FW_WARPS), WT, 0, st>>>(
-          op.d_lists + b, (int)n, op.d_tasks, op.d_A, op.d_maps, ws);
-      ++nk;
-    }
-    range(Plan::L_WIDE, b, n);
-    if (n > 0 && tma_wide) {
-      BF_TRY(launch_fwd_tma(op.d_lists + b, (int)n, op.d_tasks, op.d_A, op.d_maps, ws, op.d_err,
-                            op.ctx->prop.multiProcessorCount, st));
-      ++nk;
-    } else if (n > 0) {
-      fwd_wide_kernel<<<(unsigned)n, 256, 0, st>>>(op.d_lists + b, op.d_tasks, op.d_A,
-                                                   op.d_maps, ws);
-      ++nk;
-    }
-    range(Plan::L_COPY, b, n);
-    if (n > 0) {
-      copy_kernel<<<(unsigned)((n + 7) / 8), 256, 0, st>>>(op.d_lists + b, (int)n, op.d_tasks,
-                                                           op.d_maps, ws, 0);
-      ++nk;
-    }
-    return nk;
-  }
+  if (trans == BF_OP_N)
+    return op.d_A2 ? launch_fwd_stage<float2>(op, s, st, ws, op.d_A2)
+                   : launch_fwd_stage<float4>(op, s, st, ws, op.d_A);
   // adjoint / transpose: same tasks, rows and columns swapped
-  nk = launch_adj_stage(p, s, trans == BF_OP_C, op.d_lists, op.d_tasks, op.d_A, op.d_maps, ws,
-                        st);
+  nk = launch_adj_stage(p, s, trans == BF_OP_C, op.d_lists, op.d_tasks, op.d_A, op.d_A2,
+                        op.d_maps, ws, st);
   if (nk < 0) return 0;
   int64_t b = p.list_begin[Plan::L_COPY][s], n = p.list_begin[Plan::L_COPY][s + 1] - b;
   if (n > 0) {

@@ -36,6 +36,7 @@
 #include <memory>
 #include <numeric>
 
+#include "bf_dfloat.cuh"
 #include "bf_internal.h"
 #include "bf_umma.cuh"
 
@@ -88,8 +89,9 @@ namespace {
 // ---------------------------------------------------------------- packing
 // One CTA per (task, column block): float-float entries -> complex FP32 ->
 // real 2x2 form -> BF16 hi/lo, written into the core-matrix layout.
+template <typename FT>
 __global__ void mx_pack_kernel(const int2* __restrict__ items, const DTask* __restrict__ tasks,
-                               const int64_t* __restrict__ moff, const float4* __restrict__ A,
+                               const int64_t* __restrict__ moff, const FT* __restrict__ A,
                                uint8_t* __restrict__ F) {
   const int2 it = items[blockIdx.x];
   const DTask t = tasks[it.x];
@@ -101,9 +103,9 @@ __global__ void mx_pack_kernel(const int2* __restrict__ items, const DTask* __re
     const int m = bi * 8 + r, col = bj * 8 + c;
     float ar = 0.f, ai = 0.f;
     if (m < t.M && col < t.n) {
-      const float4 a = A[t.a_off + (size_t)col * t.M + m];
-      ar = a.x + a.y;
-      ai = a.z + a.w;
+      const float2 a = fac_c32(A[t.a_off + (size_t)col * t.M + m]);
+      ar = a.x;
+      ai = a.y;
     }
     const float v[2][2] = {{ar, -ai}, {ai, ar}};
     uint8_t* hi = seg + (size_t)bi * 512;
@@ -506,8 +508,12 @@ static int mixed_setup(Operator& op) {
                                 cudaMemcpyHostToDevice, st));
     for (size_t b = 0; b < items.size(); b += (1u << 30)) {
       const size_t nb = std::min<size_t>(items.size() - b, 1u << 30);
-      mx_pack_kernel<<<(unsigned)nb, 128, 0, st>>>(d_items + b, op.d_tasks, ms->d_moff, op.d_A,
-                                                   ms->d_F);
+      if (op.d_A2)
+        mx_pack_kernel<float2><<<(unsigned)nb, 128, 0, st>>>(d_items + b, op.d_tasks, ms->d_moff,
+                                                             op.d_A2, ms->d_F);
+      else
+        mx_pack_kernel<float4><<<(unsigned)nb, 128, 0, st>>>(d_items + b, op.d_tasks, ms->d_moff,
+                                                             op.d_A, ms->d_F);
     }
     BF_TRY_CUDA(cudaGetLastError());
     BF_TRY_CUDA(cudaStreamSynchronize(st));

@@ -76,12 +76,15 @@ struct DSU {
 
 }  // namespace
 
-int pack_plan(const Logical& lg, Plan& plan) {
+int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
   plan = Plan();
   plan.n_rows = lg.n_rows;
   plan.n_cols = lg.n_cols;
+  plan.fac_bytes = fac_bytes;
   const auto& B = lg.blocks;
   int64_t nb = (int64_t)B.size();
+  plan.blk_pk_off.assign(nb, -1);
+  plan.blk_pk_ld.assign(nb, 0);
   int32_t n_bf = lg.n_bf;
   plan.n_bf = n_bf;
   if (nb == 0 || n_bf <= 0) {
@@ -426,8 +429,10 @@ int pack_plan(const Logical& lg, Plan& plan) {
             g.src_ld = k.raw_ld;
             g.rows = k.rows;
             g.cols = k.cols;
+            plan.blk_pk_off[m.blk] = g.dst_off;
+            plan.blk_pk_ld[m.blk] = g.dst_ld;
             plan.block_entries += (int64_t)k.rows * k.cols;
-            sbytes += 16 * (int64_t)k.rows * k.cols;
+            sbytes += (int64_t)plan.fac_bytes * k.rows * k.cols;
             plan.max_rank = std::max<int64_t>(plan.max_rank, k.rows);
           }
           if (g.rows > 0 && g.cols > 0) plan.segs.push_back(g);
@@ -497,9 +502,11 @@ int pack_plan(const Logical& lg, Plan& plan) {
   plan.xg_covered = std::all_of(xcov.begin(), xcov.end(), [](uint8_t c) { return c != 0; });
   int64_t slot_total = 0;
   for (int64_t s = 0; s < n_slots; ++s) slot_total += std::max<int64_t>(slot_len[s], 0);
-  // algorithmic bytes of one forward matvec (factor entries + x read + y write +
-  // every level slot written once and read once), 16 B per complex entry
-  plan.alg_bytes_fwd = 16 * (plan.block_entries + lg.n_rows + lg.n_cols + 2 * slot_total);
+  // algorithmic bytes of one forward matvec: factor entries (fac_bytes each:
+  // 16 float-float, 8 complex FP32) + x read + y write + every level slot
+  // written once and read once (16 B per float-float vector entry)
+  plan.alg_bytes_fwd = (int64_t)plan.fac_bytes * plan.block_entries +
+                       16 * (lg.n_rows + lg.n_cols + 2 * slot_total);
   (void)alg;
   return BF_OK;
 }
