@@ -6,10 +6,18 @@ Default workload (one GPU): the plain FP64 far-field operator of a
 octree with <= 32 points per leaf, isFar(alpha=1) admissibility, tol 1e-4,
 one complex Gaussian right-hand side.  Factors are built on the GPU by
 bf_build before timing; a step is one forward far-field matvec over all
-653,570 butterflies.  The factor stream (~10 GB) is far larger than L2, so no
+653,570 butterflies.  The factor stream (~5 GB) is far larger than L2, so no
 explicit L2 flush is needed between steps.
 
+The same run measures the batched mixed-precision path on the same operator:
+256 right-hand sides (128 plane waves exp(-ik d.x) + 128 complex Gaussians)
+per step through bf_matvec_mixed, its error against the FP64 GPU matvec and
+against FP64 dense far-field rows on a seeded row sample (bfgpu.verify).
+``--workload sphere262k`` is the 262,144-point sphere (k ~ 90.8) with 2,048
+sampled rows.
+
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload NAME] [--no-mixed] [--no-cpu]
 
 N > 1 runs independent replicas (one per rank, launched by torch.distributed.run);
 the path has no cross-GPU exchange on a single operator.
@@ -36,10 +44,12 @@ UNIT = "matvec/s"
 
 WORKLOADS = {
     # name: (n points, max points per leaf, tol)
+    "sphere262k": (262144, 32, 1e-4),
     "sphere65k": (65536, 32, 1e-4),
     "sphere16k": (16384, 32, 1e-4),
     "sphere4k": (4096, 32, 1e-4),
 }
+DENSE_ROWS = {"sphere262k": 2048}  # sampled dense rows per workload (default 256)
 
 
 def parse():
@@ -50,6 +60,9 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="sphere65k")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg")
+    ap.add_argument("--mixed-rhs", type=int, default=256)
+    ap.add_argument("--mixed-steps", type=int, default=5)
     return ap.parse_args()
 
 
@@ -146,13 +159,118 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def peaks():
+def peaks(key="hbm_gbs"):
+    fallback = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             p = json.load(f)
-        return float(p["hbm_gbs"]), "measured"
+        return float(p[key]), "measured"
     except (OSError, KeyError, ValueError):
-        return 6800.0, "fallback"
+        return fallback[key], "fallback"
+
+
+def run_mixed(args, w, stream, world):
+    """256-RHS tensor-core matvecs through bf_matvec_mixed: throughput, accuracy, roofline."""
+    import torch
+    import bfgpu
+    from bfgpu import geometry as G
+    from bfgpu.verify import far_dense_rows, sample_rows
+    op, n, sp = w["op"], w["n"], stream.cuda_stream
+    nr = args.mixed_rhs
+    X = np.asfortranarray(np.concatenate(
+        [G.plane_waves(w["pts"], w["k"], nr // 2, seed=11),
+         G.complex_gaussian(n, 12, nrhs=nr - nr // 2)], axis=1))
+    xd = torch.from_numpy(np.ascontiguousarray(X.T)).cuda()  # column j contiguous
+    yd = torch.zeros_like(xd)
+    t0 = time.perf_counter()
+    info = op.mixed_info()  # packs the BF16 factors on first use
+    setup_s = time.perf_counter() - t0
+
+    def timed(view, steps):
+        def step():
+            view.matvec_ptr(xd.data_ptr(), n, yd.data_ptr(), n, nrhs=nr,
+                            ptr_mode=bfgpu.BF_PTR_DEVICE, stream=sp, mixed=True)
+        for _ in range(3):
+            step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    ms_adj = timed(op.adjoint(), max(2, args.mixed_steps // 2))
+    ms = timed(op, args.mixed_steps)
+    ms = max_over_ranks(ms, world)
+    Y = yd.cpu().numpy().T  # forward result of the last timed step
+    # FP64 GPU matvec on 8 columns (4 plane waves, 4 Gaussians)
+    cols = [0, 1, 2, 3, nr - 4, nr - 3, nr - 2, nr - 1]
+    x8 = xd[cols].contiguous()
+    y8 = torch.zeros_like(x8)
+    op.matvec_ptr(x8.data_ptr(), n, y8.data_ptr(), n, nrhs=8, ptr_mode=bfgpu.BF_PTR_DEVICE,
+                  stream=sp)
+    torch.cuda.synchronize()
+    Y8 = y8.cpu().numpy().T
+    err64 = max(float(np.linalg.norm(Y[:, c] - Y8[:, i]) / np.linalg.norm(Y8[:, i]))
+                for i, c in enumerate(cols))
+    # FP64 dense far-field rows on a seeded sample, all right-hand sides
+    rows = sample_rows(n, DENSE_ROWS.get(args.workload, 256), seed=2048)
+    t0 = time.perf_counter()
+    R = far_dense_rows(w["pts"], w["pts"], w["tree"], w["tree"], w["far"], w["k"], rows, X)
+    dense_s = time.perf_counter() - t0
+    err_dense = float(np.linalg.norm(Y[rows] - R) / np.linalg.norm(R))
+    err_dense_col = float(max(np.linalg.norm(Y[rows, j] - R[:, j]) / np.linalg.norm(R[:, j])
+                              for j in range(nr)))
+    err_dense_64 = float(np.linalg.norm(Y8[rows] - R[:, cols]) / np.linalg.norm(R[:, cols]))
+    # e2e: pinned host X and Y, copies inside the call
+    xh = torch.from_numpy(np.ascontiguousarray(X.T)).pin_memory()
+    yh = torch.zeros_like(xh).pin_memory()
+    op.matvec_ptr(xh.data_ptr(), n, yh.data_ptr(), n, nrhs=nr, ptr_mode=bfgpu.BF_PTR_HOST,
+                  mixed=True)
+    t0 = time.perf_counter()
+    e2e_steps = max(2, args.mixed_steps // 2)
+    for _ in range(e2e_steps):
+        op.matvec_ptr(xh.data_ptr(), n, yh.data_ptr(), n, nrhs=nr, ptr_mode=bfgpu.BF_PTR_HOST,
+                      mixed=True)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_s = max_over_ranks(e2e_s, world)
+    # per-level roofline (one 128-RHS chunk, CUDA events in the library)
+    sms, sby, sfl, nk = op.profile_mixed(nrep=2)
+    dom = int(np.argmax(sms))
+    hbm, hbm_kind = peaks("hbm_gbs")
+    tc, tc_kind = peaks("bf16_tflops")
+    ach_gbs = float(sby[dom] / (sms[dom] * 1e-3) / 1e9)
+    useful_tf = float(sfl[dom] / (sms[dom] * 1e-3) / 1e12)
+    tot_bytes = float(sby.sum()) * math.ceil(nr / 128)
+    return {
+        "value": world * nr * 1000.0 / ms, "unit": UNIT, "rhs_per_step": nr,
+        "ms_per_step": ms, "dtype": "bf16 hi/lo x3 on tcgen05, fp32 accumulate",
+        "rhs": f"{nr // 2} plane waves exp(-ik d.x) + {nr - nr // 2} complex Gaussians",
+        "rel_err_vs_fp64_gpu": err64,
+        "rel_err_vs_dense_rows": err_dense, "max_col_rel_err_vs_dense_rows": err_dense_col,
+        "fp64_rel_err_vs_dense_rows": err_dense_64, "dense_rows": int(len(rows)),
+        "dense_rows_seconds": round(dense_s, 2),
+        "adjoint": {"value": world * nr * 1000.0 / ms_adj, "unit": UNIT, "ms_per_step": ms_adj},
+        "hbm_gbs": tot_bytes / (ms * 1e-3) / 1e9,
+        "e2e": {"value": world * nr / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 16 * n * nr,
+                "d2h_bytes_per_step": 16 * n * nr},
+        "roofline": {"bound": "hbm", "achieved": ach_gbs, "peak": hbm, "unit": "GB/s",
+                     "frac": ach_gbs / hbm, "peak_source": f"{hbm_kind} hbm_gbs",
+                     "kernel": f"mx_level_kernel, level {dom} of {len(sms)}, one 128-RHS chunk, "
+                               f"{sms[dom]:.3f} ms",
+                     "tensor_useful_tflops": useful_tf,
+                     "tensor_pipe_tflops": 3.0 * useful_tf,
+                     "tensor_peak_tflops": tc, "tensor_peak_source": f"{tc_kind} bf16_tflops",
+                     "tensor_pipe_frac": 3.0 * useful_tf / tc,
+                     "stage_ms": [round(float(v), 4) for v in sms],
+                     "stage_bytes": [int(v) for v in sby],
+                     "stage_useful_tflop": [round(float(v) / 1e12, 4) for v in sfl]},
+        "factor_bytes_bf16": info["factor_bytes"], "workspace_bytes": info["workspace_bytes"],
+        "work_units": info["work_units"], "setup_seconds": round(setup_s, 2),
+        "gpu_launches": int(nk * math.ceil(nr / 128) * args.mixed_steps),
+    }
 
 
 def committed_traffic(workload):
@@ -309,7 +427,9 @@ def run_ours(args, rank, world, local):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64 (float-float on FP32 pipes)", "data": "synthetic",
+        "vs_baseline": None,
+        "dtype": "f64 (float-float vectors and sums on FP32 pipes; factors complex FP32 as built)",
+        "data": "synthetic",
         "config": {
             "workload": f"{args.workload}: Fibonacci sphere N={n}, k={w['k']:.2f}, "
                         f"octree<=32/leaf, isFar(1.0), tol={w['tol']}, 1 complex Gaussian RHS",
@@ -335,6 +455,9 @@ def run_ours(args, rank, world, local):
         "gpu_launches": int(kernels * args.steps),
         "clocks": clocks,
     }
+    if not args.no_mixed:
+        line["mixed"] = run_mixed(args, w, stream, world)
+        line["mixed"]["over_plain"] = line["mixed"]["value"] / value
     if rank == 0 and not args.no_cpu:
         try:
             cb, ycpu = cpu_baseline(w)
