@@ -63,7 +63,38 @@ def parse():
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg")
     ap.add_argument("--mixed-rhs", type=int, default=256)
     ap.add_argument("--mixed-steps", type=int, default=5)
+    ap.add_argument("--ncu-case", action="store_true",
+                    help="no timing: build, then 2 plain forward matvecs and 2 mixed forward "
+                         "128-RHS chunks (a short, predictable launch sequence for ncu)")
     return ap.parse_args()
+
+
+def run_ncu_case(args, local):
+    import torch
+    import bfgpu
+    from bfgpu import geometry as G
+    torch.cuda.set_device(local)
+    w = build_workload(args.workload, local)
+    op, n = w["op"], w["n"]
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sp = stream.cuda_stream
+    xd = torch.from_numpy(w["x"]).cuda()
+    yd = torch.zeros_like(xd)
+    for _ in range(2):
+        op.matvec_ptr(xd.data_ptr(), n, yd.data_ptr(), n, ptr_mode=bfgpu.BF_PTR_DEVICE, stream=sp)
+    torch.cuda.synchronize()
+    out = {"ncu_case": args.workload, "levels": op.stats()["n_stages"]}
+    if not args.no_mixed:
+        op.mixed_info()
+        X = np.ascontiguousarray(G.complex_gaussian(n, 12, nrhs=128).T)
+        xm = torch.from_numpy(X).cuda()
+        ym = torch.zeros_like(xm)
+        for _ in range(2):
+            op.matvec_ptr(xm.data_ptr(), n, ym.data_ptr(), n, nrhs=128,
+                          ptr_mode=bfgpu.BF_PTR_DEVICE, stream=sp, mixed=True)
+        torch.cuda.synchronize()
+    print(json.dumps(out), flush=True)
 
 
 def dist_setup(n_gpus):
@@ -473,7 +504,9 @@ def run_ours(args, rank, world, local):
 def main():
     args = parse()
     rank, world, local = dist_setup(args.gpus)
-    if args.impl == "reference":
+    if args.ncu_case:
+        run_ncu_case(args, local)
+    elif args.impl == "reference":
         run_reference(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
