@@ -28,8 +28,8 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import (BF_OP_C, BF_OP_N, BF_OP_T, BF_PTR_DEVICE, BF_PTR_HOST, BFError, BuildOpts,
-                   FactorDesc, OpStats, check, load)
+from ._lib import (BF_OP_C, BF_OP_N, BF_OP_T, BF_PTR_DEVICE, BF_PTR_HOST, RANK_REC_LEN, SUR_NW,
+                   BFError, BuildOpts, FactorDesc, OpStats, check, load)
 
 __all__ = ["Tree", "Context", "Operator", "nearandfar", "assemble_BF", "PetrovGalerkinBF",
            "import_blocks", "mul", "BFError", "load"]
@@ -268,11 +268,12 @@ class Operator:
         return out
 
     def rank_log(self) -> np.ndarray:
-        """Per-compression rank records of the build, (n, 14) float64 (see bfgpu.h)."""
+        """Per-compression rank records of the build, (n, 18) float64 (see bfgpu.h):
+        columns 0-13 as the reference RankLogger fields, 14-17 the surrogate features."""
         lib = load()
         n = C.c_int64()
         check(lib.bf_op_rank_log(self._h, C.byref(n), None), "rank_log")
-        rec = np.zeros((max(n.value, 1), 14))
+        rec = np.zeros((max(n.value, 1), RANK_REC_LEN))
         check(lib.bf_op_rank_log(self._h, C.byref(n), _p(rec, C.c_double)), "rank_log")
         return rec[:n.value]
 
@@ -392,6 +393,10 @@ def _build(obs, src, tree_o: Tree, tree_s: Tree, pairs, k, tol, c_tau, adaptive,
     o.keep_mixed = int(bool(keep_mixed))
     w = None
     if surrogate is not None:
+        # a bfgpu.surrogate.RankSurrogate (weights + margin) or a bare weight vector
+        if hasattr(surrogate, "weights"):
+            o.surrogate_margin = float(surrogate.margin)
+            surrogate = surrogate.weights
         w = np.ascontiguousarray(surrogate, np.float32)
         o.surrogate_weights = w.ctypes.data_as(C.POINTER(C.c_float))
         o.surrogate_nweights = w.size

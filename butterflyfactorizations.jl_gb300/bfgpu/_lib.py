@@ -10,6 +10,8 @@ LIB_PATH = os.path.join(_HERE, "libbfgpu.so")
 BF_OK, BF_EINVAL, BF_ENOMEM, BF_ECUDA, BF_ETIMEOUT, BF_ENOTSUP, BF_ESTATE = range(7)
 BF_OP_N, BF_OP_C, BF_OP_T = 0, 1, 2
 BF_PTR_HOST, BF_PTR_DEVICE = 0, 1
+RANK_REC_LEN = 18  # BF_RANK_REC_LEN
+SUR_NW = 4553      # rank-surrogate weight count (bf_surrogate_nweights)
 
 i32, i64, u64, f64, vp = C.c_int32, C.c_int64, C.c_uint64, C.c_double, C.c_void_p
 P = C.POINTER
@@ -18,7 +20,12 @@ P = C.POINTER
 class BuildOpts(C.Structure):
     _fields_ = [("c_tau", f64), ("min_samples", i32), ("adaptive", i32), ("seed", u64),
                 ("rank_mode", i32), ("keep_mixed", i32), ("surrogate_weights", P(C.c_float)),
-                ("surrogate_nweights", i64)]
+                ("surrogate_nweights", i64), ("surrogate_margin", f64)]
+
+
+class TrainOpts(C.Structure):
+    _fields_ = [("epochs", i32), ("batch", i32), ("lr", C.c_float), ("beta1", C.c_float),
+                ("beta2", C.c_float), ("eps", C.c_float), ("seed", u64)]
 
 
 class FactorDesc(C.Structure):
@@ -34,7 +41,9 @@ class OpStats(C.Structure):
     _fields_ = [("n_bf", i64), ("n_stages", i64), ("n_tasks", i64), ("factor_entries", i64),
                 ("factor_bytes", i64), ("workspace_entries", i64), ("map_entries", i64),
                 ("alg_bytes_fwd", i64), ("max_rank", i64), ("build_seconds", f64),
-                ("compressions", i64), ("retries", i64), ("kernel_entries", i64)]
+                ("compressions", i64), ("retries", i64), ("kernel_entries", i64),
+                ("build_compress_seconds", f64), ("build_pack_seconds", f64),
+                ("build_upload_seconds", f64), ("surrogate_fallbacks", i64)]
 
 
 # (name, restype, argtypes): every function declared in include/bfgpu.h
@@ -54,6 +63,14 @@ SIGNATURES = [
     ("bf_nearandfar", C.c_int, [vp, vp, f64, i32, i32, i32, P(i64), P(i64), i64, P(i64),
                                 P(i64)]),
     ("bf_build_opts_default", None, [P(BuildOpts)]),
+    ("bf_train_opts_default", None, [P(TrainOpts)]),
+    ("bf_surrogate_nweights", C.c_int, []),
+    ("bf_surrogate_init", C.c_int, [P(C.c_float), i64, u64, P(C.c_float)]),
+    ("bf_surrogate_grad", C.c_int, [vp, P(C.c_float), P(C.c_float), P(C.c_float), i64,
+                                    P(C.c_float), P(C.c_float)]),
+    ("bf_surrogate_train", C.c_int, [vp, P(C.c_float), P(C.c_float), i64, P(TrainOpts),
+                                     P(C.c_float), P(C.c_float)]),
+    ("bf_surrogate_predict", C.c_int, [vp, P(C.c_float), P(C.c_float), i64, P(C.c_float)]),
     ("bf_build", C.c_int, [vp, P(f64), i64, P(f64), i64, vp, vp, P(i64), P(i64), i64, f64, f64,
                            P(BuildOpts), P(vp)]),
     ("bf_import_factors", C.c_int, [vp, P(FactorDesc), P(vp)]),

@@ -108,6 +108,18 @@ void bf_build_opts_default(bf_build_opts* o) {
   o->seed = 0;
   o->rank_mode = 0;
   o->keep_mixed = 1;
+  o->surrogate_margin = 0.15;
+}
+
+void bf_train_opts_default(bf_train_opts* o) {
+  if (!o) return;
+  o->epochs = 30;
+  o->batch = 4096;
+  o->lr = 3e-3f;
+  o->beta1 = 0.9f;
+  o->beta2 = 0.999f;
+  o->eps = 1e-8f;
+  o->seed = 0;
 }
 
 int bf_import_factors(bf_ctx_t ctx, const bf_factor_desc* d, bf_op_t* out) {
@@ -383,7 +395,7 @@ int bf_op_rank_log(bf_op_t h, int64_t* n_rec, double* rec) {
   if (!rec) return BF_OK;
   for (size_t i = 0; i < L.size(); ++i) {
     const auto& r = L[i];
-    double* o = rec + 14 * i;
+    double* o = rec + BF_RANK_REC_LEN * i;
     o[0] = r.bf;
     o[1] = r.stage;
     o[2] = (double)r.obs_node;
@@ -398,6 +410,7 @@ int bf_op_rank_log(bf_op_t h, int64_t* n_rec, double* rec) {
     o[11] = r.a_src;
     o[12] = r.dist;
     o[13] = r.k;
+    for (int q = 0; q < 4; ++q) o[14 + q] = r.feat[q];
   }
   return BF_OK;
 }

@@ -70,6 +70,8 @@ struct HTask {
   uint64_t key;
   double eps;
   int32_t rows0, rows, retries, rank;
+  int32_t n_est;            // oversampling-estimator sample count (the fallback)
+  int8_t seeded, fell_back; // rows set by the surrogate; fell back to n_est
   int64_t t_off;
   SkelRef skel;
 };
@@ -109,7 +111,7 @@ class Builder {
   ~Builder() {
     for (void* p : {(void*)d_obs_, (void*)d_src_, (void*)d_obs_perm_, (void*)d_colpool_,
                     (void*)d_ctask_, (void*)d_Z_, (void*)d_rowpool_, (void*)d_permpool_,
-                    (void*)d_skel_})
+                    (void*)d_skel_, (void*)d_sw_, (void*)d_sfeat_, (void*)d_sout_})
       if (p) cudaFree(p);
   }
 
@@ -141,13 +143,14 @@ class Builder {
     t.n_cols = n_cols;
     t.key = task_key(opts_.seed, f, stage, obs_node, src_node);
     t.eps = st.eps;
-    int32_t est = st.n_est;
-    if (surrogate_) est = surrogate_rows(f, stage, obs_node, src_node, st.n_est);
-    t.rows0 = t.rows = std::min(std::max(est, opts_.min_samples), t.n_obs);
+    t.n_est = std::min(std::max(st.n_est, opts_.min_samples), t.n_obs);
+    t.rows0 = t.rows = t.n_est;
+    t.seeded = t.fell_back = 0;
     t.t_off = -1;
     return t;
   }
-  int32_t surrogate_rows(int32_t f, int32_t stage, int64_t o, int64_t s, int32_t fallback);
+  // surrogate-seeded sample counts for one round of compressions (GPU inference)
+  int seed_rows(std::vector<HTask>& tasks);
 
   Context* ctx_;
   const Tree& to_;
@@ -179,6 +182,10 @@ class Builder {
   int64_t raw_cap_ = 0, raw_used_ = 0;
   const Surrogate* surrogate_ = nullptr;
   Surrogate sur_;
+  float* d_sw_ = nullptr;     // surrogate weights on the device
+  float* d_sfeat_ = nullptr;  // features / predictions of one round
+  float* d_sout_ = nullptr;
+  int64_t sfeat_cap_ = 0, n_fallback_ = 0;
   // stats
   int64_t n_comp_ = 0, n_retry_ = 0, n_entries_ = 0;
 };
@@ -207,8 +214,20 @@ int Builder::ensure_raw(int64_t need) {
 // PartialQR (compressors.jl:81-165) for a batch of compressions: sample,
 // pivoted QR, adaptive doubling of the sample while r > floor(0.8 rows), then
 // the interpolation matrix and the skeleton.
+// adds the wall time of its scope to a statistics field
+struct ScopeTimer {
+  double& acc;
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  explicit ScopeTimer(double& a) : acc(a) {}
+  ~ScopeTimer() {
+    acc += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+};
+
 int Builder::run_compressions(std::vector<HTask>& tasks, const std::vector<int32_t>& colpool) {
+  ScopeTimer tm(op_.stats.build_compress_seconds);
   if (tasks.empty()) return BF_OK;
+  BF_TRY(seed_rows(tasks));
   BF_TRY(dev_reserve(d_colpool_, colpool_cap_, (int64_t)colpool.size()));
   BF_TRY_CUDA(cudaMemcpyAsync(d_colpool_, colpool.data(), colpool.size() * sizeof(int32_t),
                               cudaMemcpyHostToDevice, st_));
@@ -311,7 +330,15 @@ int Builder::run_compressions(std::vector<HTask>& tasks, const std::vector<int32
         bool retry = opts_.adaptive && t.rank > (int32_t)std::floor(0.8 * t.rows) &&
                      t.rows < t.n_obs;
         if (retry) {
-          t.rows = std::min(t.rows * 2, t.n_obs);
+          int32_t nr = t.rows * 2;
+          if (t.seeded && !t.fell_back) {
+            // the surrogate under-predicted: fall back to the oversampling
+            // estimator's count (or the doubled sample, if larger)
+            nr = std::max(nr, t.n_est);
+            t.fell_back = 1;
+            ++n_fallback_;
+          }
+          t.rows = std::min(nr, t.n_obs);
           t.retries++;
           ++n_retry_;
           next.push_back(pending[q]);
@@ -359,6 +386,7 @@ int Builder::run_compressions(std::vector<HTask>& tasks, const std::vector<int32
 
 // Dense kernel blocks K(values(Oleaf), skeleton) for the P stage (bfassembly.jl:186-197).
 int Builder::run_dense(std::vector<HTask>& tasks, const std::vector<int32_t>& colpool) {
+  ScopeTimer tm(op_.stats.build_compress_seconds);
   if (tasks.empty()) return BF_OK;
   BF_TRY(dev_reserve(d_colpool_, colpool_cap_, (int64_t)colpool.size()));
   BF_TRY_CUDA(cudaMemcpyAsync(d_colpool_, colpool.data(), colpool.size() * sizeof(int32_t),
@@ -393,16 +421,44 @@ int Builder::run_dense(std::vector<HTask>& tasks, const std::vector<int32_t>& co
   return BF_OK;
 }
 
-int32_t Builder::surrogate_rows(int32_t f, int32_t stage, int64_t o, int64_t s, int32_t fallback) {
-  const BFState& st = bfs_[f];
-  float feat[4];
-  surrogate_features(to_, ts_, k_, stage, o, s, feat);
-  float lr = sur_.predict_log_rank(feat);
-  int32_t r = (int32_t)std::ceil(std::exp((double)lr));
-  // sample enough rows that the predicted rank stays below the 0.8 retry line
-  int32_t rows = (int32_t)std::ceil(r / 0.8) + 2;
-  (void)st;
-  return std::max(rows, std::min(fallback, opts_.min_samples));
+// Surrogate-seeded sample counts for one round: features of every task (host),
+// one batched inference launch, rows = ceil(exp(pred + margin) / 0.8) + 2 so
+// that the predicted rank stays under the 0.8 x rows retry line of
+// compressors.jl:134; at least min_samples, at most the observer count.
+int Builder::seed_rows(std::vector<HTask>& tasks) {
+  if (!surrogate_ || tasks.empty()) return BF_OK;
+  const int64_t n = (int64_t)tasks.size();
+  std::vector<float> feat(4 * n), pred(n);
+  for (int64_t q = 0; q < n; ++q) {
+    const HTask& t = tasks[q];
+    surrogate_features(to_, ts_, k_, t.stage, t.obs_node, t.src_node, &feat[4 * q]);
+  }
+  if (n > sfeat_cap_) {
+    if (d_sfeat_) cudaFree(d_sfeat_);
+    if (d_sout_) cudaFree(d_sout_);
+    d_sfeat_ = d_sout_ = nullptr;
+    sfeat_cap_ = 0;
+    BF_TRY_CUDA(cudaMalloc(&d_sfeat_, (size_t)n * 4 * sizeof(float)));
+    BF_TRY_CUDA(cudaMalloc(&d_sout_, (size_t)n * sizeof(float)));
+    sfeat_cap_ = n;
+  }
+  BF_TRY_CUDA(cudaMemcpyAsync(d_sfeat_, feat.data(), feat.size() * sizeof(float),
+                              cudaMemcpyHostToDevice, st_));
+  BF_TRY(surrogate_predict_gpu(d_sw_, d_sfeat_, d_sout_, n, st_));
+  BF_TRY_CUDA(cudaMemcpyAsync(pred.data(), d_sout_, (size_t)n * sizeof(float),
+                              cudaMemcpyDeviceToHost, st_));
+  BF_TRY_CUDA(cudaStreamSynchronize(st_));
+  const double margin = opts_.surrogate_margin;
+  for (int64_t q = 0; q < n; ++q) {
+    HTask& t = tasks[q];
+    double r = std::exp(std::min((double)pred[q] + margin, 30.0));
+    int64_t rows = (int64_t)std::ceil(r / 0.8) + 2;
+    rows = std::max<int64_t>(rows, opts_.min_samples);
+    rows = std::min<int64_t>(rows, t.n_obs);
+    t.rows0 = t.rows = (int32_t)rows;
+    t.seeded = 1;
+  }
+  return BF_OK;
 }
 
 int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, int64_t n_src,
@@ -416,6 +472,8 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
       return BF_EINVAL;
     }
     surrogate_ = &sur_;
+    BF_TRY_CUDA(cudaMalloc(&d_sw_, SUR_NW * sizeof(float)));
+    BF_TRY_CUDA(cudaMemcpy(d_sw_, sur_.w.data(), SUR_NW * sizeof(float), cudaMemcpyHostToDevice));
   }
   // device copies of the geometry and of the observer permutation
   BF_TRY_CUDA(cudaMalloc(&d_obs_, (size_t)n_obs * 3 * sizeof(double)));
@@ -486,6 +544,7 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
     }
     r.dist = (float)std::sqrt(d2);
     r.k = (float)k_;
+    surrogate_features(to_, ts_, k_, t.stage, t.obs_node, t.src_node, r.feat);
     op_.rank_log.push_back(r);
   };
 
@@ -687,6 +746,7 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
   d_raw_ = nullptr;
   op_.stats.compressions = n_comp_;
   op_.stats.retries = n_retry_;
+  op_.stats.surrogate_fallbacks = n_fallback_;
   op_.stats.kernel_entries = n_entries_;
   return BF_OK;
 }
@@ -704,11 +764,19 @@ int build_operator(Context* ctx, const double* obs_xyz, int64_t n_obs, const dou
     BF_TRY(b.run(obs_xyz, n_obs, src_xyz, n_src, far_obs, far_src, n_far));
   }
   // the build's factors are complex FP32 values: packed as such (exact)
+  auto tp = std::chrono::steady_clock::now();
   BF_TRY(pack_plan(op.logical, op.plan, op.raw_is_double ? (int)sizeof(float4) : (int)sizeof(float2)));
-  BF_TRY(upload_plan(op));
+  auto tu = std::chrono::steady_clock::now();
+  const double compress_s = op.stats.build_compress_seconds;
+  const int64_t fallbacks = op.stats.surrogate_fallbacks;
+  BF_TRY(upload_plan(op));  // rewrites the plan statistics
   BF_TRY_CUDA(cudaDeviceSynchronize());
   auto t1 = std::chrono::steady_clock::now();
   op.stats.build_seconds = std::chrono::duration<double>(t1 - t0).count();
+  op.stats.build_compress_seconds = compress_s;
+  op.stats.build_pack_seconds = std::chrono::duration<double>(tu - tp).count();
+  op.stats.build_upload_seconds = std::chrono::duration<double>(t1 - tu).count();
+  op.stats.surrogate_fallbacks = fallbacks;
   return BF_OK;
 }
 

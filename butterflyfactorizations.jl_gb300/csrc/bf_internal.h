@@ -190,6 +190,7 @@ struct Operator {
     int64_t obs_node, src_node;
     int32_t n_obs, n_cols, rows0, rows, retries, rank;
     float a_obs, a_src, dist, k;
+    float feat[4];  // rank-surrogate features (bf_surrogate.h)
   };
   std::vector<RankRec> rank_log;
   ~Operator();

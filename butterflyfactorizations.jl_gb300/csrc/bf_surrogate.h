@@ -47,10 +47,10 @@ struct Surrogate {
     w.assign(p, p + n);
     for (float v : w)
       if (!std::isfinite(v)) return false;
+    for (int i = 0; i < 4; ++i)
+      if (!(w[4 + i] > 0.f)) return false;  // normalisation scales
     return true;
   }
-  // host evaluation of the same network (used for small batches and checks)
-  float predict_log_rank(const float f[4]) const;
 };
 
 // GPU inference of a batch of feature rows (features: n x 4, out: n)

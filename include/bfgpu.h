@@ -123,6 +123,8 @@ typedef struct {
   int32_t keep_mixed;    /* 1 = also keep complex-FP32 factors for bf_matvec_mixed */
   const float* surrogate_weights; /* MLP weights when rank_mode == 1 (else NULL)   */
   int64_t surrogate_nweights;
+  double surrogate_margin; /* log-rank safety margin of surrogate-seeded sample
+                              counts: rows = ceil(exp(pred + margin) / 0.8) + 2 */
 } bf_build_opts;
 
 BF_API void bf_build_opts_default(bf_build_opts* opts);
@@ -131,6 +133,39 @@ BF_API int bf_build(bf_ctx_t ctx, const double* obs_xyz, int64_t n_obs, const do
                     int64_t n_src, bf_tree_t obs_tree, bf_tree_t src_tree,
                     const int64_t* far_obs, const int64_t* far_src, int64_t n_far, double k,
                     double tol, const bf_build_opts* opts, bf_op_t* out);
+
+/* ------------------------------------------------------------------------
+ * Learned rank surrogate (no reference counterpart; it replaces the fixed
+ * ButterflyRankEstimator sample count, rankestimation.jl:93-98, whose
+ * under-estimates cost the adaptive re-sampling of compressors.jl:134-151).
+ * A 4 -> 64 -> 64 -> 1 MLP (tanh-form GELU; FP32 master weights rounded to
+ * BF16 in every evaluation, FP32 accumulation) maps the features of a
+ * compression (columns 14..17 of a rank record) to log(rank).  Weight vector:
+ * bf_surrogate_nweights() floats (normalisation mu[4], sigma[4], W1[64][4],
+ * b1[64], W2[64][64], b2[64], w3[64], b3).  All buffers are host memory. */
+typedef struct {
+  int32_t epochs;  /* passes over the records                          */
+  int32_t batch;   /* samples per Adam step                            */
+  float lr;        /* Adam step size                                   */
+  float beta1, beta2, eps;
+  uint64_t seed;   /* shuffling seed                                   */
+} bf_train_opts;
+
+BF_API void bf_train_opts_default(bf_train_opts* opts);
+BF_API int bf_surrogate_nweights(void);
+/* normalisation from the features (n x 4), Glorot-uniform layers from seed */
+BF_API int bf_surrogate_init(const float* features, int64_t n, uint64_t seed, float* weights);
+/* mean 0.5 (y - target)^2 over the n samples and its gradient (GPU kernels) */
+BF_API int bf_surrogate_grad(bf_ctx_t ctx, const float* weights, const float* features,
+                             const float* targets, int64_t n, float* grad, float* loss);
+/* Adam training on the GPU; weights in: initial, out: trained; optional
+ * loss_per_epoch[epochs] (mean batch loss of each epoch) */
+BF_API int bf_surrogate_train(bf_ctx_t ctx, const float* features, const float* targets,
+                              int64_t n, const bf_train_opts* opts, float* weights,
+                              float* loss_per_epoch);
+/* predicted log(rank) of n feature rows (GPU kernel) */
+BF_API int bf_surrogate_predict(bf_ctx_t ctx, const float* weights, const float* features,
+                                int64_t n, float* out);
 
 /* ------------------------------------------------------------------------
  * Import of factors built elsewhere (the parity path): a set of
@@ -228,6 +263,12 @@ typedef struct {
   int64_t compressions;      /* partial-QR compressions performed               */
   int64_t retries;           /* adaptive re-samplings                           */
   int64_t kernel_entries;    /* Helmholtz entries evaluated during the build    */
+  double build_compress_seconds; /* of build_seconds: compression rounds (task
+                                    arrays, GPU sampling + QR + solve, waits)     */
+  double build_pack_seconds;     /* of build_seconds: level/task packing (host)   */
+  double build_upload_seconds;   /* of build_seconds: factor repack + upload      */
+  int64_t surrogate_fallbacks;   /* surrogate-seeded compressions that fell back
+                                    to the oversampling estimator                 */
 } bf_op_stats;
 
 BF_API int bf_op_stats_get(bf_op_t op, bf_op_stats* stats);
@@ -245,10 +286,14 @@ BF_API int bf_op_export_blocks(bf_op_t op, int64_t bf_begin, int64_t bf_end, int
 
 /* Rank records of the build, one per compression (the richer form of the
  * reference RankLogger, src/ButterflyFactorization/bfstructs.jl:220-232 and
- * compressors.jl:153): 14 values per record in rec[14*i ...]:
+ * compressors.jl:153): BF_RANK_REC_LEN values per record in
+ * rec[BF_RANK_REC_LEN*i ...]:
  * bf, stage, obs_node, src_node, n_obs, n_cols, rows_initial, rows_final,
- * retries, rank, radius_obs, radius_src, center_distance, k.
+ * retries, rank, radius_obs, radius_src, center_distance, k, then the four
+ * rank-surrogate features: level, k * box diameter, separation / diameter,
+ * log(1 + points in both boxes).
  * Call with rec == NULL to query *n_rec. */
+#define BF_RANK_REC_LEN 18
 BF_API int bf_op_rank_log(bf_op_t op, int64_t* n_rec, double* rec);
 
 /* Device time of each level launch of one matvec (CUDA events on the handle's
