@@ -17,6 +17,7 @@
 #include <string>
 
 #include "bf_dfloat.cuh"
+#include "bf_fwd_warp.cuh"
 #include "bf_internal.h"
 
 namespace bfg {
@@ -90,230 +91,61 @@ __global__ void combine_kernel(double2* __restrict__ y, int64_t n, const float4*
 }
 
 // ---------------------------------------------------------------------------
-// Forward kernels, chosen per task shape by the packer (bf_pack.cpp):
-//   tall  (M > 128): warp per 128-row panel, 4 rows per lane;
+// Forward level kernels, chosen per task shape by the packer (bf_pack.cpp):
+//   tall  (M > 128): warp per 64-row panel;
 //   flat  (32 < M <= 128, n <= 256): warp per task streaming all M*n entries;
-//   small (M <= 32): warp per task, G = 32/M lane groups on interleaved columns;
-//   wide  (M <= 32, n > 2M): CTA per task (fwd_wide_kernel);
+//   small (M <= 32): warp per task, lane groups on interleaved columns;
+//   wide  (M <= 32, n > 2M): CTA per task (fwd_wide_kernel) or the bulk-copy
+//         pipeline (bf_fwd_tma.cu);
 //   copy  (identity blocks): warp per task.
-// All of them read every factor entry exactly once with coalesced 128-bit
-// loads straight from HBM; input entries are gathered once per warp into
-// shared memory and read as broadcasts.  No block-level barriers.
-constexpr int FW_WARPS = 8;
-constexpr int FW_XB = 256;  // staged input entries per warp per pass
-constexpr int TALL_RPL = TALL_ROWS / 32;  // rows per lane in the tall kernel
-
+// The warp routines are in bf_fwd_warp.cuh.  All of them read every factor
+// entry exactly once with coalesced loads straight from HBM; input entries are
+// gathered once per warp into shared memory and read as broadcasts.
 template <typename FT>
 __global__ void __launch_bounds__(FW_WARPS * 32) fwd_tall_kernel(
     const int2* __restrict__ items, int n_items, const DTask* __restrict__ tasks,
     const FT* __restrict__ A, const int32_t* __restrict__ maps, float4* __restrict__ ws) {
   __shared__ float4 xs[FW_WARPS][FW_XB];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
   const int item = blockIdx.x * FW_WARPS + warp;
   if (item >= n_items) return;
   const int2 it = items[item];
   const DTask t = tasks[it.x];
-  const int32_t* __restrict__ rmap = maps + t.rmap_off;
-  const int32_t* __restrict__ cmap = maps + t.cmap_off;
-  const int M = t.M, n = t.n;
-  float4* __restrict__ xw = xs[warp];
-  // an item covers TALL_PANELS row panels of TALL_ROWS rows; the input block
-  // is staged once when it fits (n <= FW_XB, the Q-stage case)
-  const bool one_block = n <= FW_XB;
-  if (one_block) {
-    for (int j = lane; j < n; j += 32) xw[j] = t.cbase >= 0 ? ws[t.cbase + j] : ws[cmap[j]];
-    __syncwarp();
-  }
-  for (int pnl = 0; pnl < TALL_PANELS; ++pnl) {
-  const int r0 = it.y + pnl * TALL_ROWS;
-  if (r0 >= M) break;
-  float4 acc[TALL_RPL];
-#pragma unroll
-  for (int q = 0; q < TALL_RPL; ++q) acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-  bool act[TALL_RPL];
-#pragma unroll
-  for (int q = 0; q < TALL_RPL; ++q) act[q] = r0 + lane + 32 * q < M;
-  for (int cb = 0; cb < n; cb += FW_XB) {
-    const int nb = min(FW_XB, n - cb);
-    if (!one_block) {
-      for (int j = lane; j < nb; j += 32) xw[j] = t.cbase >= 0 ? ws[t.cbase + cb + j] : ws[cmap[cb + j]];
-      __syncwarp();
-    }
-    const FT* __restrict__ ap = A + t.a_off + (size_t)cb * M + r0 + lane;
-    int j = 0;
-    // columns per iteration: 128 bytes of loads in flight per lane (eight
-    // float-float or sixteen complex FP32 entries)
-    constexpr int CPI = (sizeof(FT) == 8 ? 16 : 8) / TALL_RPL;
-    for (; j + CPI - 1 < nb; j += CPI) {
-      FT a[CPI][TALL_RPL];
-#pragma unroll
-      for (int c = 0; c < CPI; ++c)
-#pragma unroll
-        for (int q = 0; q < TALL_RPL; ++q)
-          a[c][q] = act[q] ? __ldg(ap + (size_t)c * M + 32 * q) : fac_zero<FT>();
-#pragma unroll
-      for (int c = 0; c < CPI; ++c) {
-        const float4 xc = xw[j + c];
-#pragma unroll
-        for (int q = 0; q < TALL_RPL; ++q) cdf_mac(acc[q], a[c][q], xc);
-      }
-      ap += CPI * (size_t)M;
-    }
-    for (; j + 1 < nb; j += 1) {
-      const float4 x0 = xw[j];
-#pragma unroll
-      for (int q = 0; q < TALL_RPL; ++q)
-        if (act[q]) cdf_mac(acc[q], __ldg(ap + 32 * q), x0);
-      ap += M;
-    }
-    if (j < nb) {
-      const float4 x0 = xw[j];
-#pragma unroll
-      for (int q = 0; q < TALL_RPL; ++q)
-        if (act[q]) cdf_mac(acc[q], __ldg(ap + 32 * q), x0);
-    }
-    __syncwarp();
-  }
-#pragma unroll
-  for (int q = 0; q < TALL_RPL; ++q)
-    if (act[q]) ws[rmap[r0 + lane + 32 * q]] = cdf_norm(acc[q]);
-  }  // panels
+  warp_tall<FT>(t, it.y, A, maps, ws, xs[warp]);
 }
 
-// One warp streams a whole task flat: lane l reads entry e = l + 32k of the
-// column-major M x n matrix.  With M > 32 the 32 entries of one warp load
-// belong to 32 distinct rows, so each lane adds its product into a per-row
-// accumulator in warp-private shared memory without conflicts.
 template <typename FT>
 __global__ void __launch_bounds__(FW_WARPS * 32) fwd_flat_kernel(
     const int32_t* __restrict__ tlist, int n_tasks, const DTask* __restrict__ tasks,
     const FT* __restrict__ A, const int32_t* __restrict__ maps, float4* __restrict__ ws) {
   __shared__ float4 xs[FW_WARPS][FLAT_NMAX];
   __shared__ float4 as[FW_WARPS][FLAT_MMAX];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
   const int ti = blockIdx.x * FW_WARPS + warp;
   if (ti >= n_tasks) return;
   const DTask t = tasks[tlist[ti]];
-  const int32_t* __restrict__ rmap = maps + t.rmap_off;
-  const int32_t* __restrict__ cmap = maps + t.cmap_off;
-  const int M = t.M, n = t.n;
-  float4* __restrict__ xw = xs[warp];
-  float4* __restrict__ aw = as[warp];
-  for (int j = lane; j < n; j += 32) xw[j] = t.cbase >= 0 ? ws[t.cbase + j] : ws[cmap[j]];
-  for (int i = lane; i < M; i += 32) aw[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-  __syncwarp();
-  const long long tot = (long long)M * n;
-  const FT* __restrict__ ap = A + t.a_off;
-  int row = lane, col = 0;  // entry lane: row lane of column 0 (M > 32)
-  long long e = lane;
-  constexpr int LU = sizeof(FT) == 8 ? 8 : 4;  // loads in flight: 64 bytes per lane
-  for (; e - lane + 32 * LU <= tot; e += 32 * LU) {  // warp-uniform: whole warp steps fit
-    FT v[LU];
-#pragma unroll
-    for (int u = 0; u < LU; ++u) v[u] = __ldg(ap + e + 32 * u);
-    // lane a at step u+1 can hit the row that lane a-(M-32) updates at step
-    // u: the warp barrier orders the two read-modify-writes
-#pragma unroll
-    for (int u = 0; u < LU; ++u) {
-      float4 s = aw[row];
-      cdf_mac(s, v[u], xw[col]);
-      aw[row] = s;
-      __syncwarp();
-      row += 32;
-      if (row >= M) {
-        row -= M;
-        ++col;
-      }
-    }
-  }
-  for (; e - lane < tot; e += 32) {  // warp-uniform trip count
-    if (e < tot) {
-      float4 s = aw[row];
-      cdf_mac(s, __ldg(ap + e), xw[col]);
-      aw[row] = s;
-    }
-    __syncwarp();
-    row += 32;
-    if (row >= M) {
-      row -= M;
-      ++col;
-    }
-  }
-  __syncwarp();
-  for (int i = lane; i < M; i += 32) ws[rmap[i]] = cdf_norm(aw[i]);
+  warp_flat<FT>(t, A, maps, ws, xs[warp], as[warp]);
 }
 
-// M <= 32: G = 32/M lane groups walk interleaved columns (one warp load reads
-// G*M contiguous entries); the groups meet in shared memory at the end.
 template <typename FT>
 __global__ void __launch_bounds__(FW_WARPS * 32) fwd_small_kernel(
     const int32_t* __restrict__ tlist, int n_tasks, const DTask* __restrict__ tasks,
     const FT* __restrict__ A, const int32_t* __restrict__ maps, float4* __restrict__ ws) {
   __shared__ float4 xs[FW_WARPS][FW_XB];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
   const int ti = blockIdx.x * FW_WARPS + warp;
   if (ti >= n_tasks) return;
   const DTask t = tasks[tlist[ti]];
-  const int32_t* __restrict__ rmap = maps + t.rmap_off;
-  const int32_t* __restrict__ cmap = maps + t.cmap_off;
-  const int M = t.M, n = t.n;
-  const int G = 32 / M;
-  const int g = lane / M, i = lane - g * M;
-  const bool active = g < G;
-  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-  float4* __restrict__ xw = xs[warp];
-  for (int cb = 0; cb < n; cb += FW_XB) {
-    const int nb = min(FW_XB, n - cb);
-    for (int j = lane; j < nb; j += 32) xw[j] = t.cbase >= 0 ? ws[t.cbase + cb + j] : ws[cmap[cb + j]];
-    __syncwarp();
-    if (active) {
-      const size_t step = (size_t)G * M;
-      const FT* __restrict__ ap = A + t.a_off + (size_t)(cb + g) * M + i;
-      int j = g;
-      constexpr int LU = sizeof(FT) == 8 ? 8 : 4;  // loads in flight
-      for (; j + (LU - 1) * G < nb; j += LU * G) {
-        FT a[LU];
-#pragma unroll
-        for (int u = 0; u < LU; ++u) a[u] = __ldg(ap + u * step);
-#pragma unroll
-        for (int u = 0; u < LU; ++u) cdf_mac(acc, a[u], xw[j + u * G]);
-        ap += LU * step;
-      }
-      for (; j < nb; j += G) {
-        cdf_mac(acc, __ldg(ap), xw[j]);
-        ap += step;
-      }
-    }
-    __syncwarp();
-  }
-  if (G > 1) {
-    xw[lane] = acc;  // reuse the staging buffer for the group reduction
-    __syncwarp();
-    if (active && g == 0) {
-      for (int q = 1; q < G; ++q) cdf_add(acc, xw[q * M + i]);
-      ws[rmap[i]] = cdf_norm(acc);
-    }
-  } else if (active) {
-    ws[rmap[i]] = cdf_norm(acc);
-  }
+  warp_small<FT>(t, A, maps, ws, xs[warp]);
 }
 
-// identity blocks: copy the input slot to the output slot
 __global__ void copy_kernel(const int32_t* __restrict__ tlist, int n_tasks,
                             const DTask* __restrict__ tasks, const int32_t* __restrict__ maps,
                             float4* __restrict__ ws, int reverse) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ti = blockIdx.x * (blockDim.x >> 5) + warp;
+  const int ti = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (ti >= n_tasks) return;
   const DTask t = tasks[tlist[ti]];
-  const int32_t* __restrict__ rmap = maps + t.rmap_off;
-  const int32_t* __restrict__ cmap = maps + t.cmap_off;
-  for (int i = lane; i < t.M; i += 32) {
-    if (reverse)
-      ws[cmap[i]] = ws[rmap[i]];
-    else
-      ws[rmap[i]] = ws[cmap[i]];
-  }
+  warp_copy(t, maps, ws, reverse);
 }
 
 // Forward for short wide tasks (M <= 32, many columns: the P stage).  One CTA

@@ -63,6 +63,7 @@ enum {
 typedef struct bf_context* bf_ctx_t;
 typedef struct bf_tree* bf_tree_t;
 typedef struct bf_operator* bf_op_t;
+typedef struct bf_batch* bf_batch_t;
 
 BF_API int bf_version(void);
 BF_API const char* bf_status_string(int status);
@@ -323,6 +324,37 @@ BF_API int bf_op_task_shapes(bf_op_t op, int64_t* n_tasks, int32_t* stage, int32
                              int32_t* M, int32_t* n);
 
 BF_API int bf_op_destroy(bf_op_t op);
+
+/* ------------------------------------------------------------------------
+ * Batches: many independent operators, each with its own number of right-hand
+ * sides, applied by one launch sequence (no reference counterpart: the
+ * reference runs each mul! and each column separately, bfmatrix.jl:10-75).
+ * Forward, FP64-accurate, y_i = A_i x_i for every operator i and column.  The
+ * level sequences are merged (one persistent launch per level for all
+ * operators) and captured once as a CUDA graph; right-hand sides run in
+ * chunks of rhs_chunk (default 8; one workspace per chunk column).  All
+ * operators must have the same factor storage (all GPU-built, or all imported).
+ * The operators must outlive the batch. */
+BF_API int bf_batch_create(bf_ctx_t ctx, bf_op_t const* ops, const int32_t* nrhs,
+                           int32_t n_ops, int32_t rhs_chunk, bf_batch_t* out);
+/* Device buffers of operator i: x (n_cols x nrhs) and y (n_rows x nrhs),
+ * complex double, column-major, leading dimension = size.  bf_batch_run reads
+ * every x buffer and writes every y buffer. */
+BF_API int bf_batch_buffers(bf_batch_t b, int32_t op, double** x_dev, double** y_dev);
+/* one graph launch on stream (NULL: the batch's own stream, synchronised) */
+BF_API int bf_batch_run(bf_batch_t b, void* stream);
+/* copies x[i] (ldx[i] >= n_cols_i; NULL ldx: packed) in, runs, copies y[i] out;
+ * ptr_mode BF_PTR_HOST or BF_PTR_DEVICE */
+BF_API int bf_batch_matvec(bf_batch_t b, const double* const* x, const int64_t* ldx,
+                           double* const* y, const int64_t* ldy, int ptr_mode, void* stream);
+/* Autotuner: times nrep graph replays for every candidate of (flat/tall task
+ * cut at M = 64, 96 or 128; item order longest-first or bucketed by task
+ * shape; 2, 4 or 6 persistent CTAs per SM), keeps the fastest.
+ * best_cfg[3] = {flat_mmax, bucketed, ctas_per_sm}. */
+BF_API int bf_batch_autotune(bf_batch_t b, int32_t nrep, double* best_ms, int32_t* best_cfg);
+BF_API int bf_batch_info(bf_batch_t b, int64_t* graph_nodes, int64_t* work_items,
+                         int64_t* workspace_bytes, int32_t* rhs_chunks);
+BF_API int bf_batch_destroy(bf_batch_t b);
 
 #ifdef __cplusplus
 }
