@@ -41,15 +41,17 @@ struct KKey {
   int64_t s, o;
   bool operator==(const KKey& k) const { return bf == k.bf && s == k.s && o == k.o; }
 };
-struct KKeyHash {
-  size_t operator()(const KKey& k) const {
-    return (size_t)mix64((uint64_t)k.bf * 0x9E3779B97F4A7C15ull ^ mix64((uint64_t)k.s) ^
-                         ((uint64_t)k.o << 1));
-  }
-};
 struct SkelRef {
   int64_t off = 0;
   int32_t len = 0;
+};
+
+// the skeleton map K (bfassembly.jl:76-77): (bf, source node, observer node) -> skeleton
+struct KMap {
+  FlatMap<SkelRef> m;
+  static uint64_t lo(const KKey& k) { return ((uint64_t)k.s << 32) | (uint64_t)(uint32_t)k.o; }
+  const SkelRef& at(const KKey& k) const { return m.at((uint64_t)(uint32_t)k.bf, lo(k)); }
+  void set(const KKey& k, const SkelRef& v) { m.put((uint64_t)(uint32_t)k.bf, lo(k), v); }
 };
 
 struct BFState {
@@ -160,7 +162,7 @@ class Builder {
   Operator& op_;
   cudaStream_t st_ = nullptr;
   std::vector<BFState> bfs_;
-  std::unordered_map<KKey, SkelRef, KKeyHash> K_;
+  KMap K_;
   std::vector<int32_t> skel_;  // host skeleton pool (point ids)
   // device
   double* d_obs_ = nullptr;
@@ -503,6 +505,8 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
     s.n_est = std::max((int32_t)std::ceil(opts_.c_tau * std::log(1.0 / s.eps)), 10);
     Lmax = std::max(Lmax, s.L);
   }
+  PhaseLog blog;
+  blog.mark("build: setup + far-pair state");
   Logical& lg = op_.logical;
   lg.n_rows = to_.n_points;
   lg.n_cols = ts_.n_points;
@@ -564,10 +568,11 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
     for (const HTask& t : tasks) {
       add_block(t.bf, 0, t.obs_node, t.src_node, t.obs_node, t.src_node, t.rank, t.n_cols, 0,
                 t.t_off, t.rank);
-      K_[KKey{t.bf, t.src_node, t.obs_node}] = t.skel;
+      K_.set(KKey{t.bf, t.src_node, t.obs_node}, t.skel);
       log_task(t);
     }
   }
+  blog.mark("build: Q stage");
   // ---- R levels (bfassembly.jl:107-181)
   for (int32_t l = 1; l < Lmax; ++l) {
     std::vector<HTask> tasks;
@@ -676,7 +681,9 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
           }
       }
     }
+    blog.mark("build: R level host prep");
     BF_TRY(run_compressions(tasks, pool));
+    blog.mark("build: R level compressions");
     // emit blocks, then apply the skeleton updates (deferred as in bfassembly.jl:177-180)
     std::vector<std::pair<KKey, SkelRef>> upd;
     upd.reserve(items.size());
@@ -703,7 +710,8 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
       upd.push_back({KKey{it.bf, it.upd_s, it.upd_o}, t.skel});
     }
     for (const HTask& t : tasks) log_task(t);
-    for (auto& u : upd) K_[u.first] = u.second;
+    blog.mark("build: R level emit");
+    for (auto& u : upd) K_.set(u.first, u.second);
   }
   // ---- P stage (bfassembly.jl:186-197)
   {
@@ -730,6 +738,7 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
       add_block(t.bf, -1, t.obs_node, t.src_node, t.obs_node, t.src_node, t.n_obs, t.n_cols, 0,
                 t.t_off, t.n_obs);
   }
+  blog.mark("build: P stage");
   // node -> values maps for the packer
   auto fill_vm = [](ValuesMap& vm, const Tree& t) {
     vm.ptr.assign(t.nn() + 1, 0);

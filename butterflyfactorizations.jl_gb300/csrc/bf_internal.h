@@ -3,7 +3,11 @@
 
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -30,6 +34,79 @@ const char* last_error();
     int s_ = (call);              \
     if (s_ != BF_OK) return s_;   \
   } while (0)
+
+// Open-addressing hash map from a 128-bit key (two uint64) to V, linear
+// probing, no erase: the host bookkeeping of the builder and the packer
+// inserts millions of keys, where node-based maps spend most of their time in
+// allocation and pointer chasing.
+template <typename V>
+struct FlatMap {
+  std::vector<uint64_t> khi, klo;
+  std::vector<V> val;
+  std::vector<uint8_t> used;
+  uint64_t mask = 0;
+  size_t count = 0;
+  static uint64_t mix(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  }
+  void reserve(size_t n) {
+    size_t cap = 16;
+    while (cap < 2 * n + 16) cap <<= 1;
+    if (cap <= used.size()) return;
+    FlatMap<V> t;
+    t.khi.assign(cap, 0);
+    t.klo.assign(cap, 0);
+    t.val.assign(cap, V());
+    t.used.assign(cap, 0);
+    t.mask = cap - 1;
+    for (size_t i = 0; i < used.size(); ++i)
+      if (used[i]) t.put(khi[i], klo[i], val[i]);
+    *this = std::move(t);
+  }
+  size_t slot(uint64_t hi, uint64_t lo) const {
+    size_t i = (size_t)(mix(hi ^ mix(lo)) & mask);
+    while (used[i] && (khi[i] != hi || klo[i] != lo)) i = (i + 1) & mask;
+    return i;
+  }
+  V* find(uint64_t hi, uint64_t lo) {
+    if (used.empty()) return nullptr;
+    size_t i = slot(hi, lo);
+    return used[i] ? &val[i] : nullptr;
+  }
+  const V& at(uint64_t hi, uint64_t lo) const {
+    size_t i = used.empty() ? 0 : slot(hi, lo);
+    if (used.empty() || !used[i]) throw std::out_of_range("FlatMap::at");
+    return val[i];
+  }
+  void put(uint64_t hi, uint64_t lo, const V& v) {
+    if (2 * (count + 1) > used.size()) reserve(count + 1);
+    size_t i = slot(hi, lo);
+    if (!used[i]) {
+      used[i] = 1;
+      khi[i] = hi;
+      klo[i] = lo;
+      ++count;
+    }
+    val[i] = v;
+  }
+};
+
+// Host phase timings, printed to stderr when BFGPU_TIMING is set.
+struct PhaseLog {
+  bool on;
+  std::chrono::steady_clock::time_point t;
+  PhaseLog() : on(std::getenv("BFGPU_TIMING") != nullptr), t(std::chrono::steady_clock::now()) {}
+  void mark(const char* what) {
+    if (!on) return;
+    auto n = std::chrono::steady_clock::now();
+    std::fprintf(stderr, "[bfgpu] %-32s %8.3f s\n", what,
+                 std::chrono::duration<double>(n - t).count());
+    t = n;
+  }
+};
 
 // ---------------------------------------------------------------- trees
 struct Tree {

@@ -18,29 +18,11 @@
 #include <algorithm>
 #include <cstring>
 #include <numeric>
-#include <unordered_map>
 
 #include "bf_internal.h"
 
 namespace bfg {
 namespace {
-
-struct SlotKey {
-  int32_t bf, level;
-  int64_t o, s;
-  bool operator==(const SlotKey& k) const {
-    return bf == k.bf && level == k.level && o == k.o && s == k.s;
-  }
-};
-struct SlotKeyHash {
-  size_t operator()(const SlotKey& k) const {
-    uint64_t h = 0x9E3779B97F4A7C15ull * (uint64_t)(uint32_t)k.bf;
-    h ^= (uint64_t)k.level + 0x7F4A7C159E3779B9ull + (h << 6) + (h >> 2);
-    h ^= (uint64_t)k.o * 0xBF58476D1CE4E5B9ull + (h << 6) + (h >> 2);
-    h ^= (uint64_t)k.s * 0x94D049BB133111EBull + (h << 6) + (h >> 2);
-    return (size_t)h;
-  }
-};
 
 enum : int8_t { SIDE_SLOT = 0, SIDE_X = 1, SIDE_Y = 2 };
 struct Side {
@@ -106,25 +88,32 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
     }
   }
   int32_t Lmax = *std::max_element(nlev.begin(), nlev.end());
-  // block order by (stage rank, original order): Q, R1, R2, ..., P
-  auto srank = [&](const LBlock& k) { return k.stage < 0 ? 1 << 30 : k.stage; };
+  // block order by (stage rank, original order): Q, R1, R2, ..., P -- a
+  // counting sort over the Lmax + 1 stage ranks (stable)
   std::vector<int64_t> order(nb);
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int64_t a, int64_t b) { return srank(B[a]) < srank(B[b]); });
+  {
+    auto srank = [&](const LBlock& k) { return k.stage < 0 ? Lmax : k.stage; };
+    std::vector<int64_t> cnt(Lmax + 2, 0);
+    for (int64_t b = 0; b < nb; ++b) ++cnt[srank(B[b]) + 1];
+    for (int32_t r = 0; r <= Lmax; ++r) cnt[r + 1] += cnt[r];
+    for (int64_t b = 0; b < nb; ++b) order[cnt[srank(B[b])]++] = b;
+  }
 
+  PhaseLog plog;
   // ---- slot wiring (bfstructs.jl:107-143)
-  std::unordered_map<SlotKey, int64_t, SlotKeyHash> slot_of;
-  slot_of.reserve((size_t)nb * 2);
+  // key (bf, level, o, s) packed exactly into 128 bits (node ids < 2^32)
+  FlatMap<int64_t> slot_of;
+  slot_of.reserve((size_t)nb);
   std::vector<int64_t> slot_len;
   std::vector<int64_t> in_slot(nb, -1), out_slot(nb, -1);
   auto get_slot = [&](int32_t bf, int32_t lvl, int64_t o, int64_t s, bool create) -> int64_t {
-    SlotKey key{bf, lvl, o, s};
-    auto it = slot_of.find(key);
-    if (it != slot_of.end()) return it->second;
+    if (o < 0 || s < 0 || o > INT32_MAX || s > INT32_MAX) return -2;
+    const uint64_t hi = ((uint64_t)(uint32_t)bf << 32) | (uint32_t)lvl;
+    const uint64_t lo = ((uint64_t)o << 32) | (uint64_t)s;
+    if (int64_t* v = slot_of.find(hi, lo)) return *v;
     if (!create) return -1;
     int64_t id = (int64_t)slot_len.size();
-    slot_of.emplace(key, id);
+    slot_of.put(hi, lo, id);
     slot_len.push_back(-1);
     return id;
   };
@@ -145,6 +134,10 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
         return BF_EINVAL;
       }
       int64_t so = get_slot(k.bf, 0, k.oo, k.so, true);
+      if (so < 0) {
+        set_error("pack: Q block %lld has node ids outside [0, 2^31)", (long long)b);
+        return BF_EINVAL;
+      }
       int64_t len = k.ident ? m : k.rows;
       if (slot_len[so] >= 0 && slot_len[so] != len) {
         set_error("pack: slot size mismatch at Q block %lld", (long long)b);
@@ -165,6 +158,10 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
         return BF_EINVAL;
       }
       int64_t so = get_slot(k.bf, k.stage, k.oo, k.so, true);
+      if (so < 0) {
+        set_error("pack: R%d block %lld has node ids outside [0, 2^31)", k.stage, (long long)b);
+        return BF_EINVAL;
+      }
       int64_t len = k.ident ? slot_len[si] : k.rows;
       if (slot_len[so] >= 0 && slot_len[so] != len) {
         set_error("pack: slot size mismatch at R%d block %lld", k.stage, (long long)b);
@@ -198,16 +195,16 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
   }
   int64_t n_slots = (int64_t)slot_len.size();
 
+  plog.mark("pack: order + slot wiring");
   // ---- tasks
   std::vector<std::vector<TaskB>> stages(Lmax + 1);
-  {  // Q stage: group by source node
-    std::unordered_map<int64_t, int64_t> gid;
+  {  // Q stage: group by source node (node ids validated above)
+    std::vector<int64_t> gid(lg.src_vals.ptr.size(), -1);
     for (int64_t b : order) {
       const LBlock& k = B[b];
       if (k.stage != 0) continue;
-      auto it = gid.find(k.si);
-      if (it == gid.end()) {
-        it = gid.emplace(k.si, (int64_t)stages[0].size()).first;
+      if (gid[k.si] < 0) {
+        gid[k.si] = (int64_t)stages[0].size();
         TaskB t;
         t.stage = 0;
         t.kind = TASK_DENSE;
@@ -215,32 +212,38 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
         t.cols.push_back({SIDE_X, k.si, t.n});
         stages[0].push_back(std::move(t));
       }
-      TaskB& t = stages[0][it->second];
+      TaskB& t = stages[0][gid[k.si]];
       int64_t r = slot_len[out_slot[b]];
       t.mats.push_back({k.ident ? -1 : b, (int32_t)t.M, 0, k.ident ? (int32_t)t.n : 0});
       t.rows.push_back({SIDE_SLOT, out_slot[b], r});
       t.M += r;
     }
   }
+  plog.mark("pack: Q tasks");
+  // per-slot bookkeeping shared by all R levels: a slot is a row at exactly one
+  // level (the one that writes it) and a column at exactly one level (the one
+  // that reads it), so row/column offsets need no reset; the DSU index of a
+  // slot is stamped with its level
+  std::vector<int32_t> row_off(n_slots, -1), col_off(n_slots, -1);
+  std::vector<int64_t> slot_dsu(n_slots, -1);
+  std::vector<int32_t> slot_lvl(n_slots, -1);
   for (int32_t l = 1; l < Lmax; ++l) {  // R levels: connected components over slots
     std::vector<int64_t> lb;
     for (int64_t b : order)
       if (B[b].stage == l) lb.push_back(b);
     if (lb.empty()) continue;
-    std::unordered_map<int64_t, int64_t> local;  // slot -> dsu index
     DSU d;
     auto idx = [&](int64_t slot) {
-      auto it = local.find(slot);
-      if (it != local.end()) return it->second;
+      if (slot_lvl[slot] == l) return slot_dsu[slot];
       int64_t i = (int64_t)d.p.size();
       d.p.push_back(i);
-      local.emplace(slot, i);
+      slot_lvl[slot] = l;
+      slot_dsu[slot] = i;
       return i;
     };
     for (int64_t b : lb)
       if (!B[b].ident) d.unite(idx(in_slot[b]), idx(out_slot[b]));
-    std::unordered_map<int64_t, int64_t> comp;  // dsu root -> task
-    std::unordered_map<int64_t, int32_t> row_off, col_off;  // slot -> offset in task
+    std::vector<int64_t> comp(d.p.size(), -1);  // dsu root -> task
     for (int64_t b : lb) {
       const LBlock& k = B[b];
       if (k.ident) {
@@ -255,36 +258,36 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
         continue;
       }
       int64_t root = d.find(idx(in_slot[b]));
-      auto it = comp.find(root);
-      if (it == comp.end()) {
-        it = comp.emplace(root, (int64_t)stages[l].size()).first;
+      if (comp[root] < 0) {
+        comp[root] = (int64_t)stages[l].size();
         TaskB t;
         t.stage = l;
         t.kind = TASK_DENSE;
         stages[l].push_back(std::move(t));
       }
-      TaskB& t = stages[l][it->second];
-      if (!row_off.count(out_slot[b])) {
-        row_off[out_slot[b]] = (int32_t)t.M;
-        t.rows.push_back({SIDE_SLOT, out_slot[b], slot_len[out_slot[b]]});
-        t.M += slot_len[out_slot[b]];
+      TaskB& t = stages[l][comp[root]];
+      const int64_t os = out_slot[b], is = in_slot[b];
+      if (row_off[os] < 0) {
+        row_off[os] = (int32_t)t.M;
+        t.rows.push_back({SIDE_SLOT, os, slot_len[os]});
+        t.M += slot_len[os];
       }
-      if (!col_off.count(in_slot[b])) {
-        col_off[in_slot[b]] = (int32_t)t.n;
-        t.cols.push_back({SIDE_SLOT, in_slot[b], slot_len[in_slot[b]]});
-        t.n += slot_len[in_slot[b]];
+      if (col_off[is] < 0) {
+        col_off[is] = (int32_t)t.n;
+        t.cols.push_back({SIDE_SLOT, is, slot_len[is]});
+        t.n += slot_len[is];
       }
-      t.mats.push_back({b, row_off[out_slot[b]], col_off[in_slot[b]], 0});
+      t.mats.push_back({b, row_off[os], col_off[is], 0});
     }
   }
-  {  // P stage: group by observer node
-    std::unordered_map<int64_t, int64_t> gid;
+  plog.mark("pack: R tasks");
+  {  // P stage: group by observer node (node ids validated above)
+    std::vector<int64_t> gid(lg.obs_vals.ptr.size(), -1);
     for (int64_t b : order) {
       const LBlock& k = B[b];
       if (k.stage >= 0) continue;
-      auto it = gid.find(k.oo);
-      if (it == gid.end()) {
-        it = gid.emplace(k.oo, (int64_t)stages[Lmax].size()).first;
+      if (gid[k.oo] < 0) {
+        gid[k.oo] = (int64_t)stages[Lmax].size();
         TaskB t;
         t.stage = Lmax;
         t.kind = TASK_DENSE;
@@ -292,18 +295,20 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
         t.rows.push_back({SIDE_Y, k.oo, t.M});
         stages[Lmax].push_back(std::move(t));
       }
-      TaskB& t = stages[Lmax][it->second];
+      TaskB& t = stages[Lmax][gid[k.oo]];
       int64_t c = slot_len[in_slot[b]];
       t.mats.push_back({k.ident ? -1 : b, 0, (int32_t)t.n, k.ident ? (int32_t)c : 0});
       t.cols.push_back({SIDE_SLOT, in_slot[b], c});
       t.n += c;
     }
   }
+  plog.mark("pack: P tasks");
   // big tasks first inside each launch (longest-processing-time order)
   for (auto& st : stages)
     std::stable_sort(st.begin(), st.end(),
                      [](const TaskB& a, const TaskB& b) { return a.M * a.n > b.M * b.n; });
 
+  plog.mark("pack: LPT sort");
   // ---- workspace layout: [x space | y space | slots in reader order]
   plan.xg_off = 0;
   plan.yg_off = lg.n_cols;
@@ -327,6 +332,7 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
     return BF_ENOTSUP;
   }
 
+  plog.mark("pack: workspace layout");
   // ---- leaf order of the x and y regions: the points of each Q-stage source
   // leaf (P-stage observer leaf) become one contiguous range
   std::vector<int64_t> xpos(lg.n_cols, -1), ypos(lg.n_rows, -1);
@@ -356,6 +362,7 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
     for (int64_t p = 0; p < lg.n_rows; ++p) plan.yperm[ypos[p]] = (int32_t)p;
   }
 
+  plog.mark("pack: leaf order");
   // ---- emit tasks, maps, repack segments
   std::vector<uint8_t> ycov(lg.n_rows, 0), xcov(lg.n_cols, 0);
   auto contiguous_base = [&](int64_t off, int64_t len) -> int {
@@ -365,6 +372,18 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
       if (plan.maps[off + i] != b + i) return -1;
     return b;
   };
+  {  // exact sizes of the emitted arrays
+    int64_t nmaps = 0, nsegs = 0, ntasks = 0;
+    for (int32_t s = 0; s <= Lmax; ++s)
+      for (auto& t : stages[s]) {
+        nmaps += t.M + t.n;
+        nsegs += (int64_t)t.mats.size();
+        ++ntasks;
+      }
+    plan.maps.reserve((size_t)nmaps);
+    plan.segs.reserve((size_t)nsegs);
+    plan.tasks.reserve((size_t)ntasks);
+  }
   plan.stage_begin.push_back(0);
   int64_t a_off = 0;
   int64_t alg = 0;
@@ -447,6 +466,7 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
     plan.stage_bytes.push_back(sbytes);
   }
   plan.a_entries = a_off;
+  plog.mark("pack: emit tasks/maps");
   // forward launch lists by task shape (kernels in bf_matvec.cu)
   {
     std::vector<int32_t> cls[Plan::L_NCLASS];
@@ -508,6 +528,7 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
   plan.alg_bytes_fwd = (int64_t)plan.fac_bytes * plan.block_entries +
                        16 * (lg.n_rows + lg.n_cols + 2 * slot_total);
   (void)alg;
+  plog.mark("pack: class lists + totals");
   return BF_OK;
 }
 
