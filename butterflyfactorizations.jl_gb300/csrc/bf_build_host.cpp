@@ -433,7 +433,8 @@ int Builder::seed_rows(std::vector<HTask>& tasks) {
   std::vector<float> feat(4 * n), pred(n);
   for (int64_t q = 0; q < n; ++q) {
     const HTask& t = tasks[q];
-    surrogate_features(to_, ts_, k_, t.stage, t.obs_node, t.src_node, &feat[4 * q]);
+    surrogate_features(to_, ts_, k_, t.stage, t.obs_node, t.src_node, t.n_obs, t.n_cols,
+                       &feat[4 * q]);
   }
   if (n > sfeat_cap_) {
     if (d_sfeat_) cudaFree(d_sfeat_);
@@ -548,7 +549,7 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
     }
     r.dist = (float)std::sqrt(d2);
     r.k = (float)k_;
-    surrogate_features(to_, ts_, k_, t.stage, t.obs_node, t.src_node, r.feat);
+    surrogate_features(to_, ts_, k_, t.stage, t.obs_node, t.src_node, t.n_obs, t.n_cols, r.feat);
     op_.rank_log.push_back(r);
   };
 

@@ -24,9 +24,11 @@ constexpr int SUR_IN = 4;
 constexpr int SUR_H = 64;
 constexpr int SUR_NW = 8 + SUR_H * SUR_IN + SUR_H + SUR_H * SUR_H + SUR_H + SUR_H + 1;
 
-// features of compression (stage, obs node o, src node s)
+// Features of one compression: (level, k * box diameter, centre separation /
+// diameter, log point count), the point count being that of the compressed
+// problem, min(observer points, columns) -- an upper bound of its rank.
 inline void surrogate_features(const Tree& to, const Tree& ts, double k, int stage, int64_t o,
-                               int64_t s, float f[4]) {
+                               int64_t s, int64_t n_obs, int64_t n_cols, float f[4]) {
   double ao = to.radius(o), as = ts.radius(s);
   double D = 2.0 * std::max(ao, as);
   double d2 = 0.0;
@@ -37,7 +39,7 @@ inline void surrogate_features(const Tree& to, const Tree& ts, double k, int sta
   f[0] = (float)stage;
   f[1] = (float)(k * D);
   f[2] = (float)(D > 0 ? std::sqrt(d2) / D : 0.0);
-  f[3] = (float)std::log(1.0 + (double)to.nvals(o) + (double)ts.nvals(s));
+  f[3] = (float)std::log(1.0 + (double)std::min(n_obs, n_cols));
 }
 
 struct Surrogate {

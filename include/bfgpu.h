@@ -292,7 +292,7 @@ BF_API int bf_op_export_blocks(bf_op_t op, int64_t bf_begin, int64_t bf_end, int
  * bf, stage, obs_node, src_node, n_obs, n_cols, rows_initial, rows_final,
  * retries, rank, radius_obs, radius_src, center_distance, k, then the four
  * rank-surrogate features: level, k * box diameter, separation / diameter,
- * log(1 + points in both boxes).
+ * log(1 + min(observer points, compressed columns)).
  * Call with rec == NULL to query *n_rec. */
 #define BF_RANK_REC_LEN 18
 BF_API int bf_op_rank_log(bf_op_t op, int64_t* n_rec, double* rec);
