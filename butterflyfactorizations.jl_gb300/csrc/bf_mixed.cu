@@ -23,7 +23,7 @@
 //     stored blocks as MN-major B operands (Ahat^T is the real form of A^H);
 //     the transpose conjugates inputs and outputs on top of that.
 //
-// Pipeline per CTA (4 warps, 2 CTAs per SM): two stages of shared memory,
+// Pipeline per CTA (4 warps, 3 CTAs per SM): two stages of shared memory,
 // each one input chunk (16 entries x 128 right-hand sides, hi and lo) plus the
 // matching factor blocks.  Thread 0 issues the bulk copies of the factor
 // blocks and the MMAs; all 128 threads gather and split the inputs and run
@@ -35,6 +35,7 @@
 #include <cstring>
 #include <memory>
 #include <numeric>
+#include <string>
 
 #include "bf_dfloat.cuh"
 #include "bf_internal.h"
@@ -46,11 +47,12 @@ constexpr int MX_R = 128;                         // right-hand sides per chunk 
 constexpr int MX_THREADS = 128;
 constexpr int MX_IB = 2;                          // input blocks (of 8 entries) per stage
 constexpr int MX_IC = MX_IB * 8;                  // input entries per stage
-constexpr int MX_OB = 16;                         // output blocks per unit (N <= 256)
-constexpr int MX_TCOLS = 256;                     // tensor-memory columns per CTA
+constexpr int MX_OB = 8;                          // output blocks per unit (N <= 128)
+constexpr int MX_TCOLS = 128;                     // tensor-memory columns per CTA
+constexpr int MX_CTAS_PER_SM = 3;                 // 3 x 64 KB shared memory, 3 x 128 TMEM columns
 constexpr int MX_XPLANE = (MX_IC / 4) * 2048;     // one BF16 plane of the input tile (8 KB)
 constexpr int MX_XBYTES = 2 * MX_XPLANE;          // hi + lo
-constexpr int MX_FBYTES = MX_OB * MX_IB * 1024;   // factor blocks of one stage (32 KB)
+constexpr int MX_FBYTES = MX_OB * MX_IB * 1024;   // factor blocks of one stage (16 KB)
 constexpr int MX_STAGE = MX_XBYTES + MX_FBYTES;
 constexpr int MX_NST = 2;
 constexpr size_t MX_SMEM = (size_t)MX_NST * MX_STAGE + 256;
@@ -539,7 +541,8 @@ static int mixed_stage(Operator& op, int64_t s, int trans, cudaStream_t st) {
   const int64_t b = ub[s], n = ub[s + 1] - ub[s];
   int nk = 0;
   if (n > 0) {
-    const int grid = (int)std::min<int64_t>(n, 2 * (int64_t)op.ctx->prop.multiProcessorCount);
+    const int grid = (int)std::min<int64_t>(
+        n, (int64_t)MX_CTAS_PER_SM * op.ctx->prop.multiProcessorCount);
     if (adj)
       mx_level_kernel<1><<<grid, MX_THREADS, MX_SMEM, st>>>(
           ms.d_units + b, (int)n, ms.d_counters + s, op.d_tasks, ms.d_moff, ms.d_F, op.d_maps,
