@@ -45,11 +45,11 @@ namespace bfg {
 
 constexpr int MX_R = 128;                         // right-hand sides per chunk (MMA M)
 constexpr int MX_THREADS = 128;
-constexpr int MX_IB = 2;                          // input blocks (of 8 entries) per stage
+constexpr int MX_IB = 1;                          // input blocks (of 8 entries) per stage
 constexpr int MX_IC = MX_IB * 8;                  // input entries per stage
 constexpr int MX_OB = 8;                          // output blocks per unit (N <= 128)
 constexpr int MX_TCOLS = 128;                     // tensor-memory columns per CTA
-constexpr int MX_CTAS_PER_SM = 3;                 // 3 x 64 KB shared memory, 3 x 128 TMEM columns
+constexpr int MX_CTAS_PER_SM = 4;                 // 4 x 32 KB shared memory, 4 x 128 TMEM columns
 constexpr int MX_XPLANE = (MX_IC / 4) * 2048;     // one BF16 plane of the input tile (8 KB)
 constexpr int MX_XBYTES = 2 * MX_XPLANE;          // hi + lo
 constexpr int MX_FBYTES = MX_OB * MX_IB * 1024;   // factor blocks of one stage (16 KB)
