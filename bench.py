@@ -50,7 +50,7 @@ WORKLOADS = {
     "sphere4k": (4096, 32, 1e-4),
 }
 DENSE_ROWS = {"sphere262k": 2048}  # sampled dense rows per workload (default 256)
-BATCH = {"batch32": 32}            # operator-batch workloads: number of operators
+BATCH = {"batch32": 32, "batch4": 4}  # operator-batch workloads: number of operators
 SURROGATE = {"surrogate524k": 524288}  # held-out ellipsoid size of the surrogate study
 
 
@@ -309,6 +309,15 @@ def run_ncu_case(args, local):
     import bfgpu
     from bfgpu import geometry as G
     torch.cuda.set_device(local)
+    if args.workload in BATCH:  # build the batch, replay its graph twice
+        from bfgpu.batch import Batch
+        ctx = bfgpu.Context(local)
+        ops = batch_operators(BATCH[args.workload], seed=3, ctx=ctx)
+        b = Batch([o["op"] for o in ops], [o["nrhs"] for o in ops], ctx, rhs_chunk=8)
+        b.run()
+        b.run()
+        print(json.dumps({"ncu_case": args.workload, **b.info()}), flush=True)
+        return
     w = build_workload(args.workload, local)
     op, n = w["op"], w["n"]
     stream = torch.cuda.Stream()
