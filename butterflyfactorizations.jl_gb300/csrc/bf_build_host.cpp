@@ -44,6 +44,7 @@ struct KKey {
 struct SkelRef {
   int64_t off = 0;
   int32_t len = 0;
+  int64_t slot = -1;  // level slot holding this skeleton's values (pack_plan wiring)
 };
 
 // the skeleton map K (bfassembly.jl:76-77): (bf, source node, observer node) -> skeleton
@@ -512,9 +513,19 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
   lg.n_rows = to_.n_points;
   lg.n_cols = ts_.n_points;
   lg.n_bf = (int32_t)n_far;
+  // slot ids follow the skeleton map: every new skeleton (or identity copy) of
+  // a level gets a fresh slot, blocks read the slot of the skeleton they use
+  std::vector<int64_t> slot_len;
+  auto new_slot = [&](int64_t len) {
+    slot_len.push_back(len);
+    return (int64_t)slot_len.size() - 1;
+  };
   auto add_block = [&](int32_t bf, int32_t stage, int64_t oo, int64_t so, int64_t oi, int64_t si,
-                       int32_t rows, int32_t cols, int8_t ident, int64_t raw_off, int32_t ld) {
+                       int32_t rows, int32_t cols, int8_t ident, int64_t raw_off, int32_t ld,
+                       int64_t in_slot, int64_t out_slot) {
     LBlock b;
+    b.in_slot = in_slot;
+    b.out_slot = out_slot;
     b.bf = bf;
     b.stage = stage;
     b.oo = oo;
@@ -566,9 +577,10 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
       }
     }
     BF_TRY(run_compressions(tasks, pool));
-    for (const HTask& t : tasks) {
+    for (HTask& t : tasks) {
+      t.skel.slot = new_slot(t.rank);
       add_block(t.bf, 0, t.obs_node, t.src_node, t.obs_node, t.src_node, t.rank, t.n_cols, 0,
-                t.t_off, t.rank);
+                t.t_off, t.rank, -1, t.skel.slot);
       K_.set(KKey{t.bf, t.src_node, t.obs_node}, t.skel);
       log_task(t);
     }
@@ -690,22 +702,26 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
     upd.reserve(items.size());
     for (const Item& it : items) {
       if (it.kind == 1) {
-        add_block(it.bf, l, it.oo, it.so, it.oi, it.si, 0, 0, 1, 0, 1);
-        upd.push_back({KKey{it.bf, it.upd_s, it.upd_o}, it.copy});
+        SkelRef out = it.copy;
+        out.slot = new_slot(it.copy.len);
+        add_block(it.bf, l, it.oo, it.so, it.oi, it.si, 0, 0, 1, 0, 1, it.copy.slot, out.slot);
+        upd.push_back({KKey{it.bf, it.upd_s, it.upd_o}, out});
         continue;
       }
-      const HTask& t = tasks[it.task];
+      HTask& t = tasks[it.task];
+      t.skel.slot = new_slot(t.rank);
       if (it.split_svert < 0) {
-        add_block(it.bf, l, it.oo, it.so, it.oi, it.si, t.rank, t.n_cols, 0, t.t_off, t.rank);
+        add_block(it.bf, l, it.oo, it.so, it.oi, it.si, t.rank, t.n_cols, 0, t.t_off, t.rank,
+                  K_.at(KKey{it.bf, it.si, it.oi}).slot, t.skel.slot);
       } else {
         int64_t c0 = 0;
         int64_t Sv = it.split_svert;
         for (int32_t c = 0; c < ts_.n_child[Sv]; ++c) {
           int64_t Sc = ts_.first_child[Sv] + c;
-          int32_t ks = K_.at(KKey{it.bf, Sc, it.oi}).len;
-          add_block(it.bf, l, it.oo, it.so, it.oi, Sc, t.rank, ks, 0, t.t_off + c0 * t.rank,
-                    t.rank);
-          c0 += ks;
+          const SkelRef& in = K_.at(KKey{it.bf, Sc, it.oi});
+          add_block(it.bf, l, it.oo, it.so, it.oi, Sc, t.rank, in.len, 0,
+                    t.t_off + c0 * t.rank, t.rank, in.slot, t.skel.slot);
+          c0 += in.len;
         }
       }
       upd.push_back({KKey{it.bf, it.upd_s, it.upd_o}, t.skel});
@@ -718,10 +734,12 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
   {
     std::vector<HTask> tasks;
     std::vector<int32_t> pool;
+    std::vector<int64_t> in_slots;
     for (int64_t f = 0; f < n_far; ++f) {
       const BFState& s = bfs_[f];
       for (int64_t Oleaf : s.tO.back()) {
         SkelRef ref = K_.at(KKey{(int32_t)f, s.ns, Oleaf});
+        in_slots.push_back(ref.slot);
         HTask t{};
         t.bf = (int32_t)f;
         t.obs_node = Oleaf;
@@ -735,10 +753,13 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
       }
     }
     BF_TRY(run_dense(tasks, pool));
-    for (const HTask& t : tasks)
+    for (size_t q = 0; q < tasks.size(); ++q) {
+      const HTask& t = tasks[q];
       add_block(t.bf, -1, t.obs_node, t.src_node, t.obs_node, t.src_node, t.n_obs, t.n_cols, 0,
-                t.t_off, t.n_obs);
+                t.t_off, t.n_obs, in_slots[q], -1);
+    }
   }
+  lg.slot_len = std::move(slot_len);
   blog.mark("build: P stage");
   // node -> values maps for the packer
   auto fill_vm = [](ValuesMap& vm, const Tree& t) {

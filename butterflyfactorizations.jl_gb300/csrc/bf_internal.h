@@ -139,6 +139,9 @@ struct LBlock {
   int8_t ident;
   int64_t raw_off;
   int32_t raw_ld;
+  // slot ids when the producer already knows the wiring (the GPU build);
+  // -1: derived by pack_plan from the routing keys
+  int64_t in_slot = -1, out_slot = -1;
 };
 
 // node -> values map (CSR), 0-based point indices
@@ -153,6 +156,8 @@ struct Logical {
   int32_t n_bf = 0;
   std::vector<LBlock> blocks;
   ValuesMap obs_vals, src_vals;
+  // with slot ids in the blocks: the length of every slot (else empty)
+  std::vector<int64_t> slot_len;
 };
 
 // ---------------------------------------------------------------- packed plan

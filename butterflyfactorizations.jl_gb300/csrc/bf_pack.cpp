@@ -103,7 +103,7 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
   // ---- slot wiring (bfstructs.jl:107-143)
   // key (bf, level, o, s) packed exactly into 128 bits (node ids < 2^32)
   FlatMap<int64_t> slot_of;
-  slot_of.reserve((size_t)nb);
+  if (lg.slot_len.empty()) slot_of.reserve((size_t)nb);
   std::vector<int64_t> slot_len;
   std::vector<int64_t> in_slot(nb, -1), out_slot(nb, -1);
   auto get_slot = [&](int32_t bf, int32_t lvl, int64_t o, int64_t s, bool create) -> int64_t {
@@ -120,6 +120,20 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
   auto node_ok = [&](const ValuesMap& vm, int64_t node) {
     return node >= 0 && node + 1 < (int64_t)vm.ptr.size();
   };
+  if (!lg.slot_len.empty()) {
+    // wiring supplied by the producer (the GPU build): slot ids and lengths
+    slot_len = lg.slot_len;
+    const int64_t ns = (int64_t)slot_len.size();
+    for (int64_t b = 0; b < nb; ++b) {
+      in_slot[b] = B[b].in_slot;
+      out_slot[b] = B[b].out_slot;
+      if (in_slot[b] >= ns || out_slot[b] >= ns ||
+          (B[b].stage != 0 && in_slot[b] < 0) || (B[b].stage >= 0 && out_slot[b] < 0)) {
+        set_error("pack: block %lld has invalid slot ids", (long long)b);
+        return BF_EINVAL;
+      }
+    }
+  } else
   for (int64_t b : order) {
     const LBlock& k = B[b];
     if (k.stage == 0) {
@@ -372,100 +386,128 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
       if (plan.maps[off + i] != b + i) return -1;
     return b;
   };
-  {  // exact sizes of the emitted arrays
-    int64_t nmaps = 0, nsegs = 0, ntasks = 0;
-    for (int32_t s = 0; s <= Lmax; ++s)
-      for (auto& t : stages[s]) {
-        nmaps += t.M + t.n;
-        nsegs += (int64_t)t.mats.size();
-        ++ntasks;
-      }
-    plan.maps.reserve((size_t)nmaps);
-    plan.segs.reserve((size_t)nsegs);
-    plan.tasks.reserve((size_t)ntasks);
-  }
+  // offsets of every task's maps, segments and matrix (serial prefix sums),
+  // then the tasks are emitted in parallel, each into its own ranges
+  struct TRef {
+    int32_t s;
+    int64_t i, map_off, seg_off, a_off;
+  };
+  std::vector<TRef> all;
+  int64_t n_maps = 0, n_segs = 0, a_off = 0;
   plan.stage_begin.push_back(0);
-  int64_t a_off = 0;
-  int64_t alg = 0;
   for (int32_t s = 0; s <= Lmax; ++s) {
-    int64_t sbytes = 0;
-    for (auto& t : stages[s]) {
-      sbytes += 16 * (t.M + t.n);
+    for (int64_t i = 0; i < (int64_t)stages[s].size(); ++i) {
+      const TaskB& t = stages[s][i];
       if (t.M > INT32_MAX || t.n > INT32_MAX) {
         set_error("pack: task too large");
         return BF_ENOTSUP;
       }
-      DTask d{};
-      d.M = (int)t.M;
-      d.n = (int)t.n;
-      d.kind = t.kind;
-      d.rmap_off = (long long)plan.maps.size();
-      auto emit = [&](const Side& sd, bool is_row) {
-        if (sd.type == SIDE_SLOT) {
-          for (int64_t i = 0; i < sd.len; ++i) plan.maps.push_back((int32_t)(slot_off[sd.id] + i));
-        } else if (sd.type == SIDE_X) {
-          const int64_t* v = lg.src_vals.v(sd.id);
-          for (int64_t i = 0; i < sd.len; ++i) {
-            plan.maps.push_back((int32_t)(plan.xg_off + xpos[v[i]]));
-            xcov[v[i]] = 1;
-          }
-        } else {
-          const int64_t* v = lg.obs_vals.v(sd.id);
-          for (int64_t i = 0; i < sd.len; ++i) {
-            plan.maps.push_back((int32_t)(plan.yg_off + ypos[v[i]]));
-            if (ycov[v[i]]) {
-              set_error("pack: output row %lld written by two P tasks", (long long)v[i]);
-              throw BF_EINVAL;
-            }
-            ycov[v[i]] = 1;
-          }
-        }
-        (void)is_row;
-      };
-      try {
-        for (auto& r : t.rows) emit(r, true);
-        d.cmap_off = (long long)plan.maps.size();
-        for (auto& c : t.cols) emit(c, false);
-      } catch (int code) {
-        return code;
-      }
-      d.rbase = contiguous_base(d.rmap_off, t.M);
-      d.cbase = contiguous_base(d.cmap_off, t.n);
+      TRef r{s, i, n_maps, n_segs, -1};
+      n_maps += t.M + t.n;
       if (t.kind == TASK_DENSE) {
-        d.a_off = a_off;
-        for (auto& m : t.mats) {
-          DSeg g{};
-          g.dst_ld = (int)t.M;
-          g.dst_off = a_off + (long long)m.col_off * t.M + m.row_off;
-          if (m.blk < 0) {
-            g.kind = 1;
-            g.rows = g.cols = m.ident_n;
-            alg += 0;
-          } else {
-            const LBlock& k = B[m.blk];
-            g.kind = 0;
-            g.src_off = k.raw_off;
-            g.src_ld = k.raw_ld;
-            g.rows = k.rows;
-            g.cols = k.cols;
-            plan.blk_pk_off[m.blk] = g.dst_off;
-            plan.blk_pk_ld[m.blk] = g.dst_ld;
-            plan.block_entries += (int64_t)k.rows * k.cols;
-            sbytes += (int64_t)plan.fac_bytes * k.rows * k.cols;
-            plan.max_rank = std::max<int64_t>(plan.max_rank, k.rows);
-          }
-          if (g.rows > 0 && g.cols > 0) plan.segs.push_back(g);
-        }
+        r.a_off = a_off;
         a_off += t.M * t.n;
-      } else {
-        d.a_off = -1;
+        for (auto& m : t.mats) {
+          const int64_t rr = m.blk < 0 ? m.ident_n : B[m.blk].rows;
+          const int64_t cc = m.blk < 0 ? m.ident_n : B[m.blk].cols;
+          if (rr > 0 && cc > 0) ++n_segs;
+        }
       }
-      plan.tasks.push_back(d);
+      all.push_back(r);
     }
-    plan.stage_begin.push_back((int64_t)plan.tasks.size());
-    plan.stage_bytes.push_back(sbytes);
+    plan.stage_begin.push_back((int64_t)all.size());
   }
+  if (n_maps > (int64_t)INT32_MAX * 8) {
+    set_error("pack: routing maps too large");
+    return BF_ENOTSUP;
+  }
+  plan.maps.resize((size_t)n_maps);
+  plan.segs.resize((size_t)n_segs);
+  plan.tasks.resize(all.size());
+  std::vector<int64_t> sbytes(Lmax + 1, 0);
+  int64_t block_entries = 0, max_rank = 0;
+#pragma omp parallel for schedule(dynamic, 512) reduction(+ : block_entries) \
+    reduction(max : max_rank)
+  for (int64_t q = 0; q < (int64_t)all.size(); ++q) {
+    const TRef& r = all[q];
+    const TaskB& t = stages[r.s][r.i];
+    int64_t tb = 16 * (t.M + t.n);
+    DTask d{};
+    d.M = (int)t.M;
+    d.n = (int)t.n;
+    d.kind = t.kind;
+    int32_t* mp = plan.maps.data() + r.map_off;
+    auto emit = [&](const Side& sd) {
+      if (sd.type == SIDE_SLOT) {
+        for (int64_t i = 0; i < sd.len; ++i) *mp++ = (int32_t)(slot_off[sd.id] + i);
+      } else if (sd.type == SIDE_X) {
+        const int64_t* v = lg.src_vals.v(sd.id);
+        for (int64_t i = 0; i < sd.len; ++i) *mp++ = (int32_t)(plan.xg_off + xpos[v[i]]);
+      } else {
+        const int64_t* v = lg.obs_vals.v(sd.id);
+        for (int64_t i = 0; i < sd.len; ++i) *mp++ = (int32_t)(plan.yg_off + ypos[v[i]]);
+      }
+    };
+    d.rmap_off = (long long)r.map_off;
+    for (auto& rw : t.rows) emit(rw);
+    d.cmap_off = (long long)(r.map_off + t.M);
+    for (auto& c : t.cols) emit(c);
+    d.rbase = contiguous_base(d.rmap_off, t.M);
+    d.cbase = contiguous_base(d.cmap_off, t.n);
+    d.a_off = r.a_off;
+    if (t.kind == TASK_DENSE) {
+      int64_t so = r.seg_off;
+      for (auto& m : t.mats) {
+        DSeg g{};
+        g.dst_ld = (int)t.M;
+        g.dst_off = r.a_off + (long long)m.col_off * t.M + m.row_off;
+        if (m.blk < 0) {
+          g.kind = 1;
+          g.rows = g.cols = m.ident_n;
+        } else {
+          const LBlock& k = B[m.blk];
+          g.kind = 0;
+          g.src_off = k.raw_off;
+          g.src_ld = k.raw_ld;
+          g.rows = k.rows;
+          g.cols = k.cols;
+          plan.blk_pk_off[m.blk] = g.dst_off;  // each block is in exactly one task
+          plan.blk_pk_ld[m.blk] = g.dst_ld;
+          block_entries += (int64_t)k.rows * k.cols;
+          tb += (int64_t)plan.fac_bytes * k.rows * k.cols;
+          max_rank = std::max<int64_t>(max_rank, k.rows);
+        }
+        if (g.rows > 0 && g.cols > 0) plan.segs[so++] = g;
+      }
+    }
+    plan.tasks[q] = d;
+#pragma omp atomic
+    sbytes[r.s] += tb;
+  }
+  plan.block_entries = block_entries;
+  plan.max_rank = max_rank;
+  plan.stage_bytes.assign(sbytes.begin(), sbytes.end());
   plan.a_entries = a_off;
+  // coverage of x and y; every output row has exactly one P-task writer
+  for (const TRef& r : all) {
+    const TaskB& t = stages[r.s][r.i];
+    for (auto& c : t.cols)
+      if (c.type == SIDE_X) {
+        const int64_t* v = lg.src_vals.v(c.id);
+        for (int64_t i = 0; i < c.len; ++i) xcov[v[i]] = 1;
+      }
+    for (auto& rw : t.rows)
+      if (rw.type == SIDE_Y) {
+        const int64_t* v = lg.obs_vals.v(rw.id);
+        for (int64_t i = 0; i < rw.len; ++i) {
+          if (ycov[v[i]]) {
+            set_error("pack: output row %lld written by two P tasks", (long long)v[i]);
+            return BF_EINVAL;
+          }
+          ycov[v[i]] = 1;
+        }
+      }
+  }
   plog.mark("pack: emit tasks/maps");
   // forward launch lists by task shape (kernels in bf_matvec.cu)
   {
@@ -527,7 +569,6 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
   // written once and read once (16 B per float-float vector entry)
   plan.alg_bytes_fwd = (int64_t)plan.fac_bytes * plan.block_entries +
                        16 * (lg.n_rows + lg.n_cols + 2 * slot_total);
-  (void)alg;
   plog.mark("pack: class lists + totals");
   return BF_OK;
 }
