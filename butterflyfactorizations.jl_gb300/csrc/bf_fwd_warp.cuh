@@ -5,14 +5,15 @@
 // ws[rows] = A_t * ws[cols] with the row / column slots addressed through the
 // routing maps (or a contiguous base), reading every factor entry once with
 // coalesced loads and staging the inputs in warp-private shared memory
-// (xw: FW_XB entries, aw: FLAT_MMAX row accumulators).  They are shared by the
-// per-shape level kernels (bf_matvec.cu) and by the persistent batch kernel
-// that runs the levels of many operators at once (bf_batch.cu).
+// (xw: FW_XB entries, aw: FLAT_MMAX row accumulators).  They are the level
+// routines of the per-shape kernels (bf_matvec.cu).  Blackwell's paired FP32
+// instructions (__ffma2_rn and relatives) were measured slower here: a pair
+// costs the FMA pipes as much as two scalar operations, and the operand
+// broadcasts they need add instructions.
 //   tall  : one 64-row panel of a task with M > 128, 2 rows per lane;
 //   flat  : 32 < M <= 128, n <= 256, the warp streams all M*n entries;
-//   small : M <= 32, G = 32/M lane groups on interleaved columns (also used
-//           for short wide tasks by the batch kernel);
-//   copy  : identity blocks.
+//   small : M <= 32, G = 32/M lane groups on interleaved columns;
+//   copy  : identity blocks (also used by the batch kernel, bf_batch.cu).
 #pragma once
 
 #include "bf_dfloat.cuh"
@@ -29,6 +30,11 @@ __device__ __forceinline__ float4 ws_in(const DTask& t, const int32_t* __restric
   return t.cbase >= 0 ? ws[t.cbase + j] : ws[cmap[j]];
 }
 
+// In all three routines the first factor batch is issued before the input
+// entries are staged (it does not depend on them), and a partial last batch is
+// loaded at once under predicates, so a warp waits on few serial latencies.
+// (Keeping two batches in flight instead was measured slower: the extra
+// registers cost more occupancy than the overlap gained.)
 template <typename FT>
 __device__ __forceinline__ void warp_tall(const DTask& t, int r0, const FT* __restrict__ A,
                                           const int32_t* __restrict__ maps,
@@ -38,50 +44,41 @@ __device__ __forceinline__ void warp_tall(const DTask& t, int r0, const FT* __re
   const int32_t* __restrict__ cmap = maps + t.cmap_off;
   const int M = t.M, n = t.n;
   if (r0 >= M) return;
-  // the input block is staged once when it fits (n <= FW_XB, the Q-stage case)
-  const bool one_block = n <= FW_XB;
-  if (one_block) {
-    for (int j = lane; j < n; j += 32) xw[j] = ws_in(t, cmap, ws, j);
-    __syncwarp();
-  }
   float4 acc[TALL_RPL];
 #pragma unroll
   for (int q = 0; q < TALL_RPL; ++q) acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
   bool act[TALL_RPL];
 #pragma unroll
   for (int q = 0; q < TALL_RPL; ++q) act[q] = r0 + lane + 32 * q < M;
+  // columns per batch: 128 bytes of factor loads per lane
+  constexpr int CPI = (sizeof(FT) == 8 ? 16 : 8) / TALL_RPL;
   for (int cb = 0; cb < n; cb += FW_XB) {
-    const int nb = min(FW_XB, n - cb);
-    if (!one_block) {
-      for (int j = lane; j < nb; j += 32) xw[j] = ws_in(t, cmap, ws, cb + j);
-      __syncwarp();
-    }
+    const int nb = min(FW_XB, n - cb);  // warp-uniform
     const FT* __restrict__ ap = A + t.a_off + (size_t)cb * M + r0 + lane;
-    int j = 0;
-    // columns per iteration: 128 bytes of loads in flight per lane (eight
-    // float-float or sixteen complex FP32 entries)
-    constexpr int CPI = (sizeof(FT) == 8 ? 16 : 8) / TALL_RPL;
-    for (; j + CPI - 1 < nb; j += CPI) {
-      FT a[CPI][TALL_RPL];
+    FT a[CPI][TALL_RPL];
+    auto load = [&](FT(&v)[CPI][TALL_RPL], int j) {
 #pragma unroll
       for (int c = 0; c < CPI; ++c)
 #pragma unroll
         for (int q = 0; q < TALL_RPL; ++q)
-          a[c][q] = act[q] ? __ldg(ap + (size_t)c * M + 32 * q) : fac_zero<FT>();
+          v[c][q] = (act[q] && j + c < nb) ? __ldg(ap + (size_t)(j + c) * M + 32 * q)
+                                           : fac_zero<FT>();
+    };
+    auto mac = [&](const FT(&v)[CPI][TALL_RPL], int j) {
 #pragma unroll
-      for (int c = 0; c < CPI; ++c) {
-        const float4 xc = xw[j + c];
+      for (int c = 0; c < CPI; ++c)
+        if (j + c < nb) {
+          const float4 xc = xw[j + c];
 #pragma unroll
-        for (int q = 0; q < TALL_RPL; ++q) cdf_mac(acc[q], a[c][q], xc);
-      }
-      ap += CPI * (size_t)M;
-    }
-    for (; j < nb; j += 1) {
-      const float4 x0 = xw[j];
-#pragma unroll
-      for (int q = 0; q < TALL_RPL; ++q)
-        if (act[q]) cdf_mac(acc[q], __ldg(ap + 32 * q), x0);
-      ap += M;
+          for (int q = 0; q < TALL_RPL; ++q) cdf_mac(acc[q], v[c][q], xc);
+        }
+    };
+    load(a, 0);
+    for (int j = lane; j < nb; j += 32) xw[j] = ws_in(t, cmap, ws, cb + j);
+    __syncwarp();
+    for (int j = 0; j < nb; j += CPI) {
+      if (j > 0) load(a, j);
+      mac(a, j);
     }
     __syncwarp();
   }
@@ -104,20 +101,19 @@ __device__ __forceinline__ void warp_flat(const DTask& t, const FT* __restrict__
   const int32_t* __restrict__ rmap = maps + t.rmap_off;
   const int32_t* __restrict__ cmap = maps + t.cmap_off;
   const int M = t.M, n = t.n;
-  for (int j = lane; j < n; j += 32) xw[j] = ws_in(t, cmap, ws, j);
-  for (int i = lane; i < M; i += 32) aw[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-  __syncwarp();
   const long long tot = (long long)M * n;
-  const FT* __restrict__ ap = A + t.a_off;
-  int row = lane, col = 0;  // entry lane: row lane of column 0 (M > 32)
-  long long e = lane;
-  constexpr int LU = sizeof(FT) == 8 ? 8 : 4;  // loads in flight: 64 bytes per lane
-  for (; e - lane + 32 * LU <= tot; e += 32 * LU) {  // warp-uniform: whole warp steps fit
-    FT v[LU];
+  const FT* __restrict__ ap = A + t.a_off + lane;
+  constexpr int LU = sizeof(FT) == 8 ? 8 : 4;  // one warp step: 32*LU entries
+  const long long nsteps = tot / (32 * LU);     // whole warp steps (warp-uniform)
+  FT a[LU];
+  auto load = [&](FT(&v)[LU], long long s) {
 #pragma unroll
-    for (int u = 0; u < LU; ++u) v[u] = __ldg(ap + e + 32 * u);
-    // lane a at step u+1 can hit the row that lane a-(M-32) updates at step
-    // u: the warp barrier orders the two read-modify-writes
+    for (int u = 0; u < LU; ++u) v[u] = __ldg(ap + s * (32 * LU) + 32 * u);
+  };
+  int row = lane, col = 0;  // entry lane: row lane of column 0 (M > 32)
+  // lane a at step u+1 can hit the row that lane a-(M-32) updates at step u:
+  // the warp barrier orders the two read-modify-writes
+  auto mac = [&](const FT(&v)[LU]) {
 #pragma unroll
     for (int u = 0; u < LU; ++u) {
       float4 s = aw[row];
@@ -130,11 +126,26 @@ __device__ __forceinline__ void warp_flat(const DTask& t, const FT* __restrict__
         ++col;
       }
     }
+  };
+  if (nsteps > 0) load(a, 0);  // does not wait for the input staging
+  for (int j = lane; j < n; j += 32) xw[j] = ws_in(t, cmap, ws, j);
+  for (int i = lane; i < M; i += 32) aw[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  __syncwarp();
+  for (long long s = 0; s < nsteps; ++s) {
+    if (s > 0) load(a, s);
+    mac(a);
   }
-  for (; e - lane < tot; e += 32) {  // warp-uniform trip count
-    if (e < tot) {
+  // the last partial warp step (fewer than 32*LU entries), loaded at once
+  const long long e0 = nsteps * (32 * LU);  // warp-uniform
+#pragma unroll
+  for (int u = 0; u < LU; ++u)
+    a[u] = e0 + lane + 32 * u < tot ? __ldg(ap + e0 + 32 * u) : fac_zero<FT>();
+#pragma unroll
+  for (int u = 0; u < LU; ++u) {
+    if (e0 + 32 * u >= tot) break;  // warp-uniform
+    if (e0 + lane + 32 * u < tot) {
       float4 s = aw[row];
-      cdf_mac(s, __ldg(ap + e), xw[col]);
+      cdf_mac(s, a[u], xw[col]);
       aw[row] = s;
     }
     __syncwarp();
@@ -163,27 +174,34 @@ __device__ __forceinline__ void warp_small(const DTask& t, const FT* __restrict_
   const int g = lane / M, i = lane - g * M;
   const bool active = g < G;
   float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  // lane group g reads columns g, g+G, g+2G, ...; a batch is LU of them (64
+  // bytes per lane)
+  constexpr int LU = sizeof(FT) == 8 ? 8 : 4;
+  const size_t step = (size_t)G * M;
   for (int cb = 0; cb < n; cb += FW_XB) {
-    const int nb = min(FW_XB, n - cb);
+    const int nb = min(FW_XB, n - cb);  // warp-uniform
+    const int nk = (nb + G - 1) / G;   // column steps of group 0 (warp-uniform)
+    const FT* __restrict__ ap = A + t.a_off + (size_t)(cb + g) * M + i;
+    FT a[LU];
+    auto load = [&](FT(&v)[LU], int k) {
+#pragma unroll
+      for (int u = 0; u < LU; ++u)
+        v[u] = (active && g + (k + u) * G < nb) ? __ldg(ap + (size_t)(k + u) * step)
+                                                : fac_zero<FT>();
+    };
+    auto mac = [&](const FT(&v)[LU], int k) {
+#pragma unroll
+      for (int u = 0; u < LU; ++u) {
+        const int j = g + (k + u) * G;
+        if (active && j < nb) cdf_mac(acc, v[u], xw[j]);
+      }
+    };
+    load(a, 0);  // the first factor batch does not wait for the input staging
     for (int j = lane; j < nb; j += 32) xw[j] = ws_in(t, cmap, ws, cb + j);
     __syncwarp();
-    if (active) {
-      const size_t step = (size_t)G * M;
-      const FT* __restrict__ ap = A + t.a_off + (size_t)(cb + g) * M + i;
-      int j = g;
-      constexpr int LU = sizeof(FT) == 8 ? 8 : 4;  // loads in flight
-      for (; j + (LU - 1) * G < nb; j += LU * G) {
-        FT a[LU];
-#pragma unroll
-        for (int u = 0; u < LU; ++u) a[u] = __ldg(ap + u * step);
-#pragma unroll
-        for (int u = 0; u < LU; ++u) cdf_mac(acc, a[u], xw[j + u * G]);
-        ap += LU * step;
-      }
-      for (; j < nb; j += G) {
-        cdf_mac(acc, __ldg(ap), xw[j]);
-        ap += step;
-      }
+    for (int k = 0; k < nk; k += LU) {
+      if (k > 0) load(a, k);
+      mac(a, k);
     }
     __syncwarp();
   }
