@@ -116,12 +116,27 @@ class Builder {
                     (void*)d_ctask_, (void*)d_Z_, (void*)d_rowpool_, (void*)d_permpool_,
                     (void*)d_skel_, (void*)d_sw_, (void*)d_sfeat_, (void*)d_sout_})
       if (p) cudaFree(p);
+    for (cudaEvent_t e : ev_)
+      if (e) cudaEventDestroy(e);
   }
 
   int run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, int64_t n_src,
           const int64_t* far_obs, const int64_t* far_src, int64_t n_far);
 
  private:
+  // device time of the compression launches (sampling, QR, triangular solve),
+  // reported with the phase times when BFGPU_TIMING is set
+  cudaEvent_t ev_[2] = {nullptr, nullptr};
+  double comp_gpu_s_ = 0;
+  int64_t comp_chunks_ = 0;
+  void gpu_span_begin() {
+    if (ev_[0]) cudaEventRecord(ev_[0], st_);
+  }
+  void gpu_span_end() {  // after the stream synchronise that follows the span
+    if (!ev_[0]) return;
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, ev_[0], ev_[1]) == cudaSuccess) comp_gpu_s_ += ms * 1e-3;
+  }
   int ensure_raw(int64_t need);
   int run_compressions(std::vector<HTask>& tasks, const std::vector<int32_t>& colpool);
   int run_dense(std::vector<HTask>& tasks, const std::vector<int32_t>& colpool);
@@ -230,6 +245,10 @@ struct ScopeTimer {
 int Builder::run_compressions(std::vector<HTask>& tasks, const std::vector<int32_t>& colpool) {
   ScopeTimer tm(op_.stats.build_compress_seconds);
   if (tasks.empty()) return BF_OK;
+  if (!ev_[0] && std::getenv("BFGPU_TIMING")) {
+    BF_TRY_CUDA(cudaEventCreate(&ev_[0]));
+    BF_TRY_CUDA(cudaEventCreate(&ev_[1]));
+  }
   BF_TRY(seed_rows(tasks));
   BF_TRY(dev_reserve(d_colpool_, colpool_cap_, (int64_t)colpool.size()));
   BF_TRY_CUDA(cudaMemcpyAsync(d_colpool_, colpool.data(), colpool.size() * sizeof(int32_t),
@@ -297,6 +316,7 @@ int Builder::run_compressions(std::vector<HTask>& tasks, const std::vector<int32
       BF_TRY(dev_reserve(d_permpool_, perm_cap_, po));
       BF_TRY_CUDA(cudaMemcpyAsync(d_ctask_, ct.data(), np * sizeof(CTask), cudaMemcpyHostToDevice,
                                   st_));
+      gpu_span_begin();
       BF_TRY(launch_rows(d_ctask_, (int)np, d_obs_perm_, d_rowpool_, st_));
       BF_TRY(launch_eval(d_ctask_, (int)np, d_obs_, d_src_, d_rowpool_, d_colpool_, d_Z_, k_, 0,
                          st_));
@@ -319,9 +339,12 @@ int Builder::run_compressions(std::vector<HTask>& tasks, const std::vector<int32
         BF_TRY(launch_qr(d_ctask_ + q0, (int)(q1 - q0), d_Z_, d_permpool_, fits, smax, st_));
         q0 = q1;
       }
+      if (ev_[1]) cudaEventRecord(ev_[1], st_);
       BF_TRY_CUDA(cudaMemcpyAsync(ct.data(), d_ctask_, np * sizeof(CTask), cudaMemcpyDeviceToHost,
                                   st_));
       BF_TRY_CUDA(cudaStreamSynchronize(st_));
+      gpu_span_end();
+      ++comp_chunks_;
       // adaptive decisions (compressors.jl:134-151)
       next.clear();
       done.clear();
@@ -372,13 +395,16 @@ int Builder::run_compressions(std::vector<HTask>& tasks, const std::vector<int32
         // done tasks reuse the front of the CTask buffer (their Z stays in place)
         BF_TRY_CUDA(cudaMemcpyAsync(d_ctask_, dct.data(), dct.size() * sizeof(CTask),
                                     cudaMemcpyHostToDevice, st_));
+        gpu_span_begin();
         BF_TRY(launch_tsolve(d_ctask_, (int)dct.size(), d_Z_, d_permpool_, d_colpool_, d_raw_,
                              d_skel_, max_rank, st_));
+        if (ev_[1]) cudaEventRecord(ev_[1], st_);
         hskel.resize(ssum);
         if (ssum > 0)
           BF_TRY_CUDA(cudaMemcpyAsync(hskel.data(), d_skel_, ssum * sizeof(int32_t),
                                       cudaMemcpyDeviceToHost, st_));
         BF_TRY_CUDA(cudaStreamSynchronize(st_));
+        gpu_span_end();
         skel_.insert(skel_.end(), hskel.begin(), hskel.end());
       }
       pending.swap(next);
@@ -761,6 +787,9 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
   }
   lg.slot_len = std::move(slot_len);
   blog.mark("build: P stage");
+  if (blog.on)
+    std::fprintf(stderr, "[bfgpu] %-32s %8.3f s (%lld chunks; inside the compression phases)\n",
+                 "compress: device time", comp_gpu_s_, (long long)comp_chunks_);
   // node -> values maps for the packer
   auto fill_vm = [](ValuesMap& vm, const Tree& t) {
     vm.ptr.assign(t.nn() + 1, 0);
