@@ -7,6 +7,7 @@
 // padded level lists, the skeleton map K (bfassembly.jl:76-77) and the block
 // keys; matrices never leave the device.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -542,11 +543,7 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
   // slot ids follow the skeleton map: every new skeleton (or identity copy) of
   // a level gets a fresh slot, blocks read the slot of the skeleton they use
   std::vector<int64_t> slot_len;
-  auto new_slot = [&](int64_t len) {
-    slot_len.push_back(len);
-    return (int64_t)slot_len.size() - 1;
-  };
-  auto add_block = [&](int32_t bf, int32_t stage, int64_t oo, int64_t so, int64_t oi, int64_t si,
+  auto make_block = [](int32_t bf, int32_t stage, int64_t oo, int64_t so, int64_t oi, int64_t si,
                        int32_t rows, int32_t cols, int8_t ident, int64_t raw_off, int32_t ld,
                        int64_t in_slot, int64_t out_slot) {
     LBlock b;
@@ -563,9 +560,9 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
     b.ident = ident;
     b.raw_off = raw_off;
     b.raw_ld = std::max(ld, 1);
-    lg.blocks.push_back(b);
+    return b;
   };
-  auto log_task = [&](const HTask& t) {
+  auto rank_rec = [&](const HTask& t) {
     Operator::RankRec r;
     r.bf = t.bf;
     r.stage = t.stage;
@@ -587,202 +584,327 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
     r.dist = (float)std::sqrt(d2);
     r.k = (float)k_;
     surrogate_features(to_, ts_, k_, t.stage, t.obs_node, t.src_node, t.n_obs, t.n_cols, r.feat);
-    op_.rank_log.push_back(r);
+    return r;
+  };
+
+  // Host loops over the far pairs run in parallel over chunks of far pairs.
+  // Each chunk fills its own buffers and the chunks are joined in far-pair
+  // order, so tasks, pools, blocks and slot ids are exactly those of a serial
+  // loop.  The skeleton map is only read inside the parallel loops; its updates
+  // are applied serially after each round.
+  const int64_t n_chunks = std::max<int64_t>(1, std::min<int64_t>(n_far, 4096));
+  struct Part {
+    std::vector<HTask> tasks;
+    std::vector<int32_t> pool;
+    std::vector<Item> items;
+    std::vector<int64_t> in_slots;
+  };
+  // body(chunk, f_begin, f_end) on every chunk; a failed skeleton-map lookup in
+  // any chunk is rethrown here (the caller turns it into BF_EINVAL)
+  auto for_chunks = [&](auto&& body) {
+    std::atomic<int> failed{0};
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t c = 0; c < n_chunks; ++c) {
+      try {
+        body(c, n_far * c / n_chunks, n_far * (c + 1) / n_chunks);
+      } catch (const std::bad_alloc&) {
+        failed = 2;
+      } catch (...) {
+        failed = 1;
+      }
+    }
+    if (failed == 2) throw std::bad_alloc();
+    if (failed) throw std::out_of_range("skeleton map lookup");
+  };
+  // chunk parts -> one round: pool offsets and task indices shift by the
+  // chunk's position
+  auto join = [&](std::vector<Part>& parts, std::vector<HTask>& tasks, std::vector<int32_t>& pool,
+                  std::vector<Item>* items, std::vector<int64_t>* in_slots) {
+    const int64_t P = (int64_t)parts.size();
+    std::vector<int64_t> tb(P + 1, 0), pb(P + 1, 0), ib(P + 1, 0);
+    for (int64_t c = 0; c < P; ++c) {
+      tb[c + 1] = tb[c] + (int64_t)parts[c].tasks.size();
+      pb[c + 1] = pb[c] + (int64_t)parts[c].pool.size();
+      ib[c + 1] = ib[c] + (int64_t)parts[c].items.size();
+    }
+    tasks.resize(tb[P]);
+    pool.resize(pb[P]);
+    if (items) items->resize(ib[P]);
+    if (in_slots) in_slots->resize(tb[P]);
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t c = 0; c < P; ++c) {
+      Part& p = parts[c];
+      for (size_t q = 0; q < p.tasks.size(); ++q) {
+        tasks[tb[c] + q] = p.tasks[q];
+        tasks[tb[c] + q].cols_off += pb[c];
+      }
+      std::copy(p.pool.begin(), p.pool.end(), pool.begin() + pb[c]);
+      if (items)
+        for (size_t q = 0; q < p.items.size(); ++q) {
+          Item it = p.items[q];
+          if (it.task >= 0) it.task += tb[c];
+          (*items)[ib[c] + q] = it;
+        }
+      if (in_slots) std::copy(p.in_slots.begin(), p.in_slots.end(), in_slots->begin() + tb[c]);
+      p = Part();
+    }
+  };
+  // rank records of one round, in task order
+  auto log_tasks = [&](const std::vector<HTask>& tasks) {
+    const size_t base = op_.rank_log.size();
+    op_.rank_log.resize(base + tasks.size());
+#pragma omp parallel for schedule(static)
+    for (int64_t q = 0; q < (int64_t)tasks.size(); ++q) op_.rank_log[base + q] = rank_rec(tasks[q]);
   };
 
   // ---- Q stage (bfassembly.jl:82-102)
   {
+    std::vector<Part> parts(n_chunks);
+    for_chunks([&](int64_t c, int64_t f0, int64_t f1) {
+      Part& p = parts[c];
+      for (int64_t f = f0; f < f1; ++f) {
+        const BFState& s = bfs_[f];
+        for (int64_t Sleaf : s.tS.back()) {
+          int64_t off = (int64_t)p.pool.size();
+          add_values(p.pool, ts_, Sleaf);
+          p.tasks.push_back(make_task((int32_t)f, 0, s.no, Sleaf, off, (int32_t)ts_.nvals(Sleaf)));
+        }
+      }
+    });
     std::vector<HTask> tasks;
     std::vector<int32_t> pool;
-    for (int64_t f = 0; f < n_far; ++f) {
-      const BFState& s = bfs_[f];
-      for (int64_t Sleaf : s.tS.back()) {
-        int64_t off = (int64_t)pool.size();
-        add_values(pool, ts_, Sleaf);
-        tasks.push_back(make_task((int32_t)f, 0, s.no, Sleaf, off, (int32_t)ts_.nvals(Sleaf)));
-      }
-    }
+    join(parts, tasks, pool, nullptr, nullptr);
     BF_TRY(run_compressions(tasks, pool));
-    for (HTask& t : tasks) {
-      t.skel.slot = new_slot(t.rank);
-      add_block(t.bf, 0, t.obs_node, t.src_node, t.obs_node, t.src_node, t.rank, t.n_cols, 0,
-                t.t_off, t.rank, -1, t.skel.slot);
-      K_.set(KKey{t.bf, t.src_node, t.obs_node}, t.skel);
-      log_task(t);
+    const int64_t nt = (int64_t)tasks.size();
+    const int64_t sb = (int64_t)slot_len.size(), bb = (int64_t)lg.blocks.size();
+    slot_len.resize(sb + nt);
+    lg.blocks.resize(bb + nt);
+#pragma omp parallel for schedule(static)
+    for (int64_t q = 0; q < nt; ++q) {
+      HTask& t = tasks[q];
+      t.skel.slot = sb + q;
+      slot_len[sb + q] = t.rank;
+      lg.blocks[bb + q] = make_block(t.bf, 0, t.obs_node, t.src_node, t.obs_node, t.src_node,
+                                     t.rank, t.n_cols, 0, t.t_off, t.rank, -1, t.skel.slot);
     }
+    for (const HTask& t : tasks) K_.set(KKey{t.bf, t.src_node, t.obs_node}, t.skel);
+    log_tasks(tasks);
   }
   blog.mark("build: Q stage");
   // ---- R levels (bfassembly.jl:107-181)
   for (int32_t l = 1; l < Lmax; ++l) {
+    std::vector<Part> parts(n_chunks);
+    for_chunks([&](int64_t c, int64_t f0, int64_t f1) {
+      Part& p = parts[c];
+      std::vector<HTask>& tasks = p.tasks;
+      std::vector<int32_t>& pool = p.pool;
+      std::vector<Item>& items = p.items;
+      auto comp_item = [&](int32_t f, int64_t obs_node, int64_t svert, int64_t cols_off,
+                           int32_t ncols, int64_t oo, int64_t so, int64_t oi, int64_t si,
+                           int64_t split, int64_t us, int64_t uo) {
+        Item it{};
+        it.kind = 0;
+        it.bf = f;
+        it.oo = oo;
+        it.so = so;
+        it.oi = oi;
+        it.si = si;
+        it.split_svert = split;
+        it.upd_s = us;
+        it.upd_o = uo;
+        it.task = (int64_t)tasks.size();
+        tasks.push_back(make_task(f, l, obs_node, svert, cols_off, ncols));
+        items.push_back(it);
+      };
+      auto ident_item = [&](int32_t f, int64_t Overt, int64_t Svert) {
+        Item it{};
+        it.kind = 1;
+        it.bf = f;
+        it.oo = it.oi = Overt;
+        it.so = it.si = Svert;
+        it.split_svert = -1;
+        it.upd_s = Svert;
+        it.upd_o = Overt;
+        it.task = -1;
+        it.copy = K_.at(KKey{f, Svert, Overt});
+        items.push_back(it);
+      };
+      // U(Svert, Overt): concatenated child skeletons (bfassembly.jl:206-230)
+      auto push_U = [&](int32_t f, int64_t Svert, int64_t Overt, int64_t& off, int32_t& len) {
+        off = (int64_t)pool.size();
+        if (!ts_.isleaf(Svert)) {
+          for (int32_t ch = 0; ch < ts_.n_child[Svert]; ++ch)
+            add_skel(pool, K_.at(KKey{f, ts_.first_child[Svert] + ch, Overt}));
+        } else {
+          add_skel(pool, K_.at(KKey{f, Svert, Overt}));
+        }
+        len = (int32_t)((int64_t)pool.size() - off);
+      };
+      for (int64_t f = f0; f < f1; ++f) {
+        const BFState& s = bfs_[f];
+        if (l >= s.L) continue;
+        const int32_t fi = (int32_t)f;
+        bool sfz = l >= s.LS, ofz = l >= s.LO;
+        if (!sfz && !ofz) {  // build_nonfrozen_R_blocks (bfassembly.jl:232-349)
+          const auto& olv = s.tO[l - 1];
+          const auto& slv = s.tS[s.LS - l - 1];
+          for (int64_t Svert : slv)
+            for (int64_t Overt : olv) {
+              bool sleaf = ts_.isleaf(Svert);
+              if (!to_.isleaf(Overt)) {
+                int64_t off;
+                int32_t len;
+                push_U(fi, Svert, Overt, off, len);
+                for (int32_t ch = 0; ch < to_.n_child[Overt]; ++ch) {
+                  int64_t Oc = to_.first_child[Overt] + ch;
+                  comp_item(fi, Oc, Svert, off, len, Oc, Svert, Overt, Svert, sleaf ? -1 : Svert,
+                            Svert, Oc);
+                }
+              } else if (!sleaf) {
+                int64_t off;
+                int32_t len;
+                push_U(fi, Svert, Overt, off, len);
+                comp_item(fi, Overt, Svert, off, len, Overt, Svert, Overt, Svert, Svert, Svert,
+                          Overt);
+              } else {
+                ident_item(fi, Overt, Svert);
+              }
+            }
+        } else if (sfz && !ofz) {  // build_sourcefrozen_R_blocks (bfassembly.jl:351-412)
+          int64_t Svert = s.ns;
+          for (int64_t Overt : s.tO[l - 1]) {
+            if (!to_.isleaf(Overt)) {
+              SkelRef ref = K_.at(KKey{fi, Svert, Overt});
+              int64_t off = (int64_t)pool.size();
+              add_skel(pool, ref);
+              for (int32_t ch = 0; ch < to_.n_child[Overt]; ++ch) {
+                int64_t Oc = to_.first_child[Overt] + ch;
+                comp_item(fi, Oc, Svert, off, ref.len, Oc, Svert, Overt, Svert, -1, Svert, Oc);
+              }
+            } else {
+              ident_item(fi, Overt, Svert);
+            }
+          }
+        } else {  // build_observerfrozen_R_blocks (bfassembly.jl:414-481)
+          const auto& olv = s.tO[s.LO - 1];
+          const auto& slv = s.tS[s.LS - l - 1];
+          for (int64_t Svert : slv)
+            for (int64_t Overt : olv) {
+              if (!ts_.isleaf(Svert)) {
+                int64_t off;
+                int32_t len;
+                push_U(fi, Svert, Overt, off, len);
+                comp_item(fi, Overt, Svert, off, len, Overt, Svert, Overt, Svert, Svert, Svert,
+                          Overt);
+              } else {
+                ident_item(fi, Overt, Svert);
+              }
+            }
+        }
+      }
+    });
     std::vector<HTask> tasks;
     std::vector<int32_t> pool;
     std::vector<Item> items;
-    auto comp_item = [&](int32_t f, int64_t obs_node, int64_t svert, int64_t cols_off,
-                         int32_t ncols, int64_t oo, int64_t so, int64_t oi, int64_t si,
-                         int64_t split, int64_t us, int64_t uo) {
-      Item it{};
-      it.kind = 0;
-      it.bf = f;
-      it.oo = oo;
-      it.so = so;
-      it.oi = oi;
-      it.si = si;
-      it.split_svert = split;
-      it.upd_s = us;
-      it.upd_o = uo;
-      it.task = (int64_t)tasks.size();
-      tasks.push_back(make_task(f, l, obs_node, svert, cols_off, ncols));
-      items.push_back(it);
-    };
-    auto ident_item = [&](int32_t f, int64_t Overt, int64_t Svert) {
-      Item it{};
-      it.kind = 1;
-      it.bf = f;
-      it.oo = it.oi = Overt;
-      it.so = it.si = Svert;
-      it.split_svert = -1;
-      it.upd_s = Svert;
-      it.upd_o = Overt;
-      it.task = -1;
-      it.copy = K_.at(KKey{f, Svert, Overt});
-      items.push_back(it);
-    };
-    // U(Svert, Overt): concatenated child skeletons (bfassembly.jl:206-230)
-    auto push_U = [&](int32_t f, int64_t Svert, int64_t Overt, int64_t& off, int32_t& len) {
-      off = (int64_t)pool.size();
-      if (!ts_.isleaf(Svert)) {
-        for (int32_t c = 0; c < ts_.n_child[Svert]; ++c)
-          add_skel(pool, K_.at(KKey{f, ts_.first_child[Svert] + c, Overt}));
-      } else {
-        add_skel(pool, K_.at(KKey{f, Svert, Overt}));
-      }
-      len = (int32_t)((int64_t)pool.size() - off);
-    };
-    for (int64_t f = 0; f < n_far; ++f) {
-      const BFState& s = bfs_[f];
-      if (l >= s.L) continue;
-      const int32_t fi = (int32_t)f;
-      bool sfz = l >= s.LS, ofz = l >= s.LO;
-      if (!sfz && !ofz) {  // build_nonfrozen_R_blocks (bfassembly.jl:232-349)
-        const auto& olv = s.tO[l - 1];
-        const auto& slv = s.tS[s.LS - l - 1];
-        for (int64_t Svert : slv)
-          for (int64_t Overt : olv) {
-            bool sleaf = ts_.isleaf(Svert);
-            if (!to_.isleaf(Overt)) {
-              int64_t off;
-              int32_t len;
-              push_U(fi, Svert, Overt, off, len);
-              for (int32_t c = 0; c < to_.n_child[Overt]; ++c) {
-                int64_t Oc = to_.first_child[Overt] + c;
-                comp_item(fi, Oc, Svert, off, len, Oc, Svert, Overt, Svert, sleaf ? -1 : Svert,
-                          Svert, Oc);
-              }
-            } else if (!sleaf) {
-              int64_t off;
-              int32_t len;
-              push_U(fi, Svert, Overt, off, len);
-              comp_item(fi, Overt, Svert, off, len, Overt, Svert, Overt, Svert, Svert, Svert,
-                        Overt);
-            } else {
-              ident_item(fi, Overt, Svert);
-            }
-          }
-      } else if (sfz && !ofz) {  // build_sourcefrozen_R_blocks (bfassembly.jl:351-412)
-        int64_t Svert = s.ns;
-        for (int64_t Overt : s.tO[l - 1]) {
-          if (!to_.isleaf(Overt)) {
-            SkelRef ref = K_.at(KKey{fi, Svert, Overt});
-            int64_t off = (int64_t)pool.size();
-            add_skel(pool, ref);
-            for (int32_t c = 0; c < to_.n_child[Overt]; ++c) {
-              int64_t Oc = to_.first_child[Overt] + c;
-              comp_item(fi, Oc, Svert, off, ref.len, Oc, Svert, Overt, Svert, -1, Svert, Oc);
-            }
-          } else {
-            ident_item(fi, Overt, Svert);
-          }
-        }
-      } else {  // build_observerfrozen_R_blocks (bfassembly.jl:414-481)
-        const auto& olv = s.tO[s.LO - 1];
-        const auto& slv = s.tS[s.LS - l - 1];
-        for (int64_t Svert : slv)
-          for (int64_t Overt : olv) {
-            if (!ts_.isleaf(Svert)) {
-              int64_t off;
-              int32_t len;
-              push_U(fi, Svert, Overt, off, len);
-              comp_item(fi, Overt, Svert, off, len, Overt, Svert, Overt, Svert, Svert, Svert,
-                        Overt);
-            } else {
-              ident_item(fi, Overt, Svert);
-            }
-          }
-      }
-    }
+    join(parts, tasks, pool, &items, nullptr);
     blog.mark("build: R level host prep");
     BF_TRY(run_compressions(tasks, pool));
     blog.mark("build: R level compressions");
-    // emit blocks, then apply the skeleton updates (deferred as in bfassembly.jl:177-180)
-    std::vector<std::pair<KKey, SkelRef>> upd;
-    upd.reserve(items.size());
-    for (const Item& it : items) {
-      if (it.kind == 1) {
-        SkelRef out = it.copy;
-        out.slot = new_slot(it.copy.len);
-        add_block(it.bf, l, it.oo, it.so, it.oi, it.si, 0, 0, 1, 0, 1, it.copy.slot, out.slot);
-        upd.push_back({KKey{it.bf, it.upd_s, it.upd_o}, out});
-        continue;
-      }
-      HTask& t = tasks[it.task];
-      t.skel.slot = new_slot(t.rank);
-      if (it.split_svert < 0) {
-        add_block(it.bf, l, it.oo, it.so, it.oi, it.si, t.rank, t.n_cols, 0, t.t_off, t.rank,
-                  K_.at(KKey{it.bf, it.si, it.oi}).slot, t.skel.slot);
-      } else {
-        int64_t c0 = 0;
-        int64_t Sv = it.split_svert;
-        for (int32_t c = 0; c < ts_.n_child[Sv]; ++c) {
-          int64_t Sc = ts_.first_child[Sv] + c;
-          const SkelRef& in = K_.at(KKey{it.bf, Sc, it.oi});
-          add_block(it.bf, l, it.oo, it.so, it.oi, Sc, t.rank, in.len, 0,
-                    t.t_off + c0 * t.rank, t.rank, in.slot, t.skel.slot);
-          c0 += in.len;
-        }
-      }
-      upd.push_back({KKey{it.bf, it.upd_s, it.upd_o}, t.skel});
+    // emit blocks, then apply the skeleton updates (deferred as in
+    // bfassembly.jl:177-180).  Every item makes one new slot (slot id = base +
+    // item index) and one block, or one block per child of a split source.
+    const int64_t ni = (int64_t)items.size();
+    std::vector<int64_t> boff(ni + 1, 0);
+#pragma omp parallel for schedule(static)
+    for (int64_t q = 0; q < ni; ++q) {
+      const Item& it = items[q];
+      boff[q + 1] = (it.kind == 0 && it.split_svert >= 0) ? ts_.n_child[it.split_svert] : 1;
     }
-    for (const HTask& t : tasks) log_task(t);
+    for (int64_t q = 0; q < ni; ++q) boff[q + 1] += boff[q];
+    const int64_t sb = (int64_t)slot_len.size(), bb = (int64_t)lg.blocks.size();
+    slot_len.resize(sb + ni);
+    lg.blocks.resize(bb + boff[ni]);
+    std::vector<std::pair<KKey, SkelRef>> upd(ni);
+    std::atomic<int> failed{0};
+#pragma omp parallel for schedule(static)
+    for (int64_t q = 0; q < ni; ++q) {
+      try {
+        const Item& it = items[q];
+        const int64_t slot = sb + q;
+        int64_t b = bb + boff[q];
+        if (it.kind == 1) {
+          SkelRef out = it.copy;
+          out.slot = slot;
+          slot_len[slot] = it.copy.len;
+          lg.blocks[b] = make_block(it.bf, l, it.oo, it.so, it.oi, it.si, 0, 0, 1, 0, 1,
+                                    it.copy.slot, slot);
+          upd[q] = {KKey{it.bf, it.upd_s, it.upd_o}, out};
+        } else {
+          HTask& t = tasks[it.task];
+          t.skel.slot = slot;
+          slot_len[slot] = t.rank;
+          if (it.split_svert < 0) {
+            lg.blocks[b] = make_block(it.bf, l, it.oo, it.so, it.oi, it.si, t.rank, t.n_cols, 0,
+                                      t.t_off, t.rank, K_.at(KKey{it.bf, it.si, it.oi}).slot, slot);
+          } else {
+            int64_t c0 = 0;
+            const int64_t Sv = it.split_svert;
+            for (int32_t ch = 0; ch < ts_.n_child[Sv]; ++ch) {
+              const int64_t Sc = ts_.first_child[Sv] + ch;
+              const SkelRef& in = K_.at(KKey{it.bf, Sc, it.oi});
+              lg.blocks[b++] = make_block(it.bf, l, it.oo, it.so, it.oi, Sc, t.rank, in.len, 0,
+                                          t.t_off + c0 * t.rank, t.rank, in.slot, slot);
+              c0 += in.len;
+            }
+          }
+          upd[q] = {KKey{it.bf, it.upd_s, it.upd_o}, t.skel};
+        }
+      } catch (...) {
+        failed = 1;
+      }
+    }
+    if (failed) throw std::out_of_range("skeleton map lookup");
+    log_tasks(tasks);
     blog.mark("build: R level emit");
     for (auto& u : upd) K_.set(u.first, u.second);
+    blog.mark("build: R level skeleton map");
   }
   // ---- P stage (bfassembly.jl:186-197)
   {
+    std::vector<Part> parts(n_chunks);
+    for_chunks([&](int64_t c, int64_t f0, int64_t f1) {
+      Part& p = parts[c];
+      for (int64_t f = f0; f < f1; ++f) {
+        const BFState& s = bfs_[f];
+        for (int64_t Oleaf : s.tO.back()) {
+          SkelRef ref = K_.at(KKey{(int32_t)f, s.ns, Oleaf});
+          p.in_slots.push_back(ref.slot);
+          HTask t{};
+          t.bf = (int32_t)f;
+          t.obs_node = Oleaf;
+          t.src_node = s.ns;
+          t.obs_begin = to_.begin[Oleaf];
+          t.n_obs = (int32_t)to_.nvals(Oleaf);
+          t.cols_off = (int64_t)p.pool.size();
+          t.n_cols = ref.len;
+          add_skel(p.pool, ref);
+          p.tasks.push_back(t);
+        }
+      }
+    });
     std::vector<HTask> tasks;
     std::vector<int32_t> pool;
     std::vector<int64_t> in_slots;
-    for (int64_t f = 0; f < n_far; ++f) {
-      const BFState& s = bfs_[f];
-      for (int64_t Oleaf : s.tO.back()) {
-        SkelRef ref = K_.at(KKey{(int32_t)f, s.ns, Oleaf});
-        in_slots.push_back(ref.slot);
-        HTask t{};
-        t.bf = (int32_t)f;
-        t.obs_node = Oleaf;
-        t.src_node = s.ns;
-        t.obs_begin = to_.begin[Oleaf];
-        t.n_obs = (int32_t)to_.nvals(Oleaf);
-        t.cols_off = (int64_t)pool.size();
-        t.n_cols = ref.len;
-        add_skel(pool, ref);
-        tasks.push_back(t);
-      }
-    }
+    join(parts, tasks, pool, nullptr, &in_slots);
     BF_TRY(run_dense(tasks, pool));
-    for (size_t q = 0; q < tasks.size(); ++q) {
+    const int64_t nt = (int64_t)tasks.size();
+    const int64_t bb = (int64_t)lg.blocks.size();
+    lg.blocks.resize(bb + nt);
+#pragma omp parallel for schedule(static)
+    for (int64_t q = 0; q < nt; ++q) {
       const HTask& t = tasks[q];
-      add_block(t.bf, -1, t.obs_node, t.src_node, t.obs_node, t.src_node, t.n_obs, t.n_cols, 0,
-                t.t_off, t.n_obs, in_slots[q], -1);
+      lg.blocks[bb + q] = make_block(t.bf, -1, t.obs_node, t.src_node, t.obs_node, t.src_node,
+                                     t.n_obs, t.n_cols, 0, t.t_off, t.n_obs, in_slots[q], -1);
     }
   }
   lg.slot_len = std::move(slot_len);
