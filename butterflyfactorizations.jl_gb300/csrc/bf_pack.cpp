@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cstring>
 #include <numeric>
+#include <parallel/algorithm>
 
 #include "bf_internal.h"
 
@@ -91,11 +92,13 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
   // block order by (stage rank, original order): Q, R1, R2, ..., P -- a
   // counting sort over the Lmax + 1 stage ranks (stable)
   std::vector<int64_t> order(nb);
+  std::vector<int64_t> sbeg(Lmax + 2, 0);  // order[sbeg[r] .. sbeg[r+1]): stage rank r
   {
     auto srank = [&](const LBlock& k) { return k.stage < 0 ? Lmax : k.stage; };
     std::vector<int64_t> cnt(Lmax + 2, 0);
     for (int64_t b = 0; b < nb; ++b) ++cnt[srank(B[b]) + 1];
     for (int32_t r = 0; r <= Lmax; ++r) cnt[r + 1] += cnt[r];
+    sbeg = cnt;
     for (int64_t b = 0; b < nb; ++b) order[cnt[srank(B[b])]++] = b;
   }
 
@@ -242,57 +245,94 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
   std::vector<int64_t> slot_dsu(n_slots, -1);
   std::vector<int32_t> slot_lvl(n_slots, -1);
   for (int32_t l = 1; l < Lmax; ++l) {  // R levels: connected components over slots
-    std::vector<int64_t> lb;
-    for (int64_t b : order)
-      if (B[b].stage == l) lb.push_back(b);
-    if (lb.empty()) continue;
-    DSU d;
-    auto idx = [&](int64_t slot) {
-      if (slot_lvl[slot] == l) return slot_dsu[slot];
-      int64_t i = (int64_t)d.p.size();
-      d.p.push_back(i);
-      slot_lvl[slot] = l;
-      slot_dsu[slot] = i;
-      return i;
-    };
-    for (int64_t b : lb)
-      if (!B[b].ident) d.unite(idx(in_slot[b]), idx(out_slot[b]));
-    std::vector<int64_t> comp(d.p.size(), -1);  // dsu root -> task
-    for (int64_t b : lb) {
-      const LBlock& k = B[b];
-      if (k.ident) {
-        TaskB t;
-        t.stage = l;
-        t.kind = TASK_COPY;
-        int64_t len = slot_len[in_slot[b]];
-        t.rows.push_back({SIDE_SLOT, out_slot[b], len});
-        t.cols.push_back({SIDE_SLOT, in_slot[b], len});
-        t.M = t.n = len;
-        stages[l].push_back(std::move(t));
-        continue;
+    const int64_t lo = sbeg[l], hi = sbeg[l + 1];
+    if (lo == hi) continue;
+    // Every slot belongs to one far pair, so no component crosses far pairs.
+    // When the level's blocks come grouped by far pair (the builder's order),
+    // the level splits at far-pair boundaries into chunks, each with its own
+    // union-find, joined in order: the same tasks in the same order as one
+    // pass.  Otherwise (an import in another order) it is one chunk.
+    std::vector<int64_t> cut{lo};
+    {
+      bool grouped = true;
+      std::vector<uint8_t> seen(lg.n_bf > 0 ? lg.n_bf : 1, 0);
+      for (int64_t i = lo; i < hi && grouped; ++i) {
+        const int32_t f = B[order[i]].bf;
+        if (i == lo || f != B[order[i - 1]].bf) {
+          if (f < 0 || f >= lg.n_bf || seen[f]) grouped = false;
+          else seen[f] = 1;
+        }
       }
-      int64_t root = d.find(idx(in_slot[b]));
-      if (comp[root] < 0) {
-        comp[root] = (int64_t)stages[l].size();
-        TaskB t;
-        t.stage = l;
-        t.kind = TASK_DENSE;
-        stages[l].push_back(std::move(t));
+      const int64_t want = grouped ? std::min<int64_t>(hi - lo, 1024) : 1;
+      for (int64_t k = 1; k < want; ++k) {
+        int64_t p = std::max(lo + (hi - lo) * k / want, cut.back() + 1);
+        while (p < hi && B[order[p]].bf == B[order[p - 1]].bf) ++p;
+        if (p >= hi) break;
+        cut.push_back(p);
       }
-      TaskB& t = stages[l][comp[root]];
-      const int64_t os = out_slot[b], is = in_slot[b];
-      if (row_off[os] < 0) {
-        row_off[os] = (int32_t)t.M;
-        t.rows.push_back({SIDE_SLOT, os, slot_len[os]});
-        t.M += slot_len[os];
-      }
-      if (col_off[is] < 0) {
-        col_off[is] = (int32_t)t.n;
-        t.cols.push_back({SIDE_SLOT, is, slot_len[is]});
-        t.n += slot_len[is];
-      }
-      t.mats.push_back({b, row_off[os], col_off[is], 0});
+      cut.push_back(hi);
     }
+    const int64_t nc = (int64_t)cut.size() - 1;
+    std::vector<std::vector<TaskB>> part(nc);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t c = 0; c < nc; ++c) {
+      DSU d;
+      std::vector<TaskB>& out = part[c];
+      auto idx = [&](int64_t slot) {
+        if (slot_lvl[slot] == l) return slot_dsu[slot];
+        int64_t i = (int64_t)d.p.size();
+        d.p.push_back(i);
+        slot_lvl[slot] = l;
+        slot_dsu[slot] = i;
+        return i;
+      };
+      for (int64_t i = cut[c]; i < cut[c + 1]; ++i) {
+        const int64_t b = order[i];
+        if (!B[b].ident) d.unite(idx(in_slot[b]), idx(out_slot[b]));
+      }
+      std::vector<int64_t> comp(d.p.size(), -1);  // dsu root -> task
+      for (int64_t i = cut[c]; i < cut[c + 1]; ++i) {
+        const int64_t b = order[i];
+        const LBlock& k = B[b];
+        if (k.ident) {
+          TaskB t;
+          t.stage = l;
+          t.kind = TASK_COPY;
+          int64_t len = slot_len[in_slot[b]];
+          t.rows.push_back({SIDE_SLOT, out_slot[b], len});
+          t.cols.push_back({SIDE_SLOT, in_slot[b], len});
+          t.M = t.n = len;
+          out.push_back(std::move(t));
+          continue;
+        }
+        int64_t root = d.find(idx(in_slot[b]));
+        if (comp[root] < 0) {
+          comp[root] = (int64_t)out.size();
+          TaskB t;
+          t.stage = l;
+          t.kind = TASK_DENSE;
+          out.push_back(std::move(t));
+        }
+        TaskB& t = out[comp[root]];
+        const int64_t os = out_slot[b], is = in_slot[b];
+        if (row_off[os] < 0) {
+          row_off[os] = (int32_t)t.M;
+          t.rows.push_back({SIDE_SLOT, os, slot_len[os]});
+          t.M += slot_len[os];
+        }
+        if (col_off[is] < 0) {
+          col_off[is] = (int32_t)t.n;
+          t.cols.push_back({SIDE_SLOT, is, slot_len[is]});
+          t.n += slot_len[is];
+        }
+        t.mats.push_back({b, row_off[os], col_off[is], 0});
+      }
+    }
+    size_t tot = stages[l].size();
+    for (auto& p : part) tot += p.size();
+    stages[l].reserve(tot);
+    for (auto& p : part)
+      for (auto& t : p) stages[l].push_back(std::move(t));
   }
   plog.mark("pack: R tasks");
   {  // P stage: group by observer node (node ids validated above)
@@ -318,9 +358,11 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
   }
   plog.mark("pack: P tasks");
   // big tasks first inside each launch (longest-processing-time order)
+  // (GCC's parallel-mode stable sort: the result of a stable sort is unique)
   for (auto& st : stages)
-    std::stable_sort(st.begin(), st.end(),
-                     [](const TaskB& a, const TaskB& b) { return a.M * a.n > b.M * b.n; });
+    __gnu_parallel::stable_sort(st.begin(), st.end(), [](const TaskB& a, const TaskB& b) {
+      return a.M * a.n > b.M * b.n;
+    });
 
   plog.mark("pack: LPT sort");
   // ---- workspace layout: [x space | y space | slots in reader order]
@@ -386,36 +428,52 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
       if (plan.maps[off + i] != b + i) return -1;
     return b;
   };
-  // offsets of every task's maps, segments and matrix (serial prefix sums),
-  // then the tasks are emitted in parallel, each into its own ranges
+  // offsets of every task's maps, segments and matrix (per-task counts in
+  // parallel, serial prefix sums), then the tasks are emitted in parallel,
+  // each into its own ranges
   struct TRef {
     int32_t s;
     int64_t i, map_off, seg_off, a_off;
   };
   std::vector<TRef> all;
-  int64_t n_maps = 0, n_segs = 0, a_off = 0;
   plan.stage_begin.push_back(0);
+  for (int32_t s = 0; s <= Lmax; ++s)
+    plan.stage_begin.push_back(plan.stage_begin.back() + (int64_t)stages[s].size());
+  all.resize((size_t)plan.stage_begin.back());
+  int too_large = 0;
   for (int32_t s = 0; s <= Lmax; ++s) {
+    const int64_t base = plan.stage_begin[s];
+#pragma omp parallel for schedule(static) reduction(| : too_large)
     for (int64_t i = 0; i < (int64_t)stages[s].size(); ++i) {
       const TaskB& t = stages[s][i];
-      if (t.M > INT32_MAX || t.n > INT32_MAX) {
-        set_error("pack: task too large");
-        return BF_ENOTSUP;
-      }
-      TRef r{s, i, n_maps, n_segs, -1};
-      n_maps += t.M + t.n;
+      if (t.M > INT32_MAX || t.n > INT32_MAX) too_large = 1;
+      // counts for now; turned into offsets below
+      TRef r{s, i, t.M + t.n, 0, 0};
       if (t.kind == TASK_DENSE) {
-        r.a_off = a_off;
-        a_off += t.M * t.n;
+        r.a_off = t.M * t.n;
         for (auto& m : t.mats) {
           const int64_t rr = m.blk < 0 ? m.ident_n : B[m.blk].rows;
           const int64_t cc = m.blk < 0 ? m.ident_n : B[m.blk].cols;
-          if (rr > 0 && cc > 0) ++n_segs;
+          if (rr > 0 && cc > 0) ++r.seg_off;
         }
       }
-      all.push_back(r);
+      all[base + i] = r;
     }
-    plan.stage_begin.push_back((int64_t)all.size());
+  }
+  if (too_large) {
+    set_error("pack: task too large");
+    return BF_ENOTSUP;
+  }
+  int64_t n_maps = 0, n_segs = 0, a_off = 0;
+  for (TRef& r : all) {
+    const int64_t nm = r.map_off, ns = r.seg_off, na = r.a_off;
+    const bool dense = stages[r.s][r.i].kind == TASK_DENSE;
+    r.map_off = n_maps;
+    r.seg_off = n_segs;
+    r.a_off = dense ? a_off : -1;
+    n_maps += nm;
+    n_segs += ns;
+    a_off += na;
   }
   if (n_maps > (int64_t)INT32_MAX * 8) {
     set_error("pack: routing maps too large");
@@ -488,25 +546,30 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
   plan.max_rank = max_rank;
   plan.stage_bytes.assign(sbytes.begin(), sbytes.end());
   plan.a_entries = a_off;
-  // coverage of x and y; every output row has exactly one P-task writer
-  for (const TRef& r : all) {
-    const TaskB& t = stages[r.s][r.i];
-    for (auto& c : t.cols)
-      if (c.type == SIDE_X) {
-        const int64_t* v = lg.src_vals.v(c.id);
-        for (int64_t i = 0; i < c.len; ++i) xcov[v[i]] = 1;
-      }
-    for (auto& rw : t.rows)
-      if (rw.type == SIDE_Y) {
-        const int64_t* v = lg.obs_vals.v(rw.id);
-        for (int64_t i = 0; i < rw.len; ++i) {
-          if (ycov[v[i]]) {
-            set_error("pack: output row %lld written by two P tasks", (long long)v[i]);
-            return BF_EINVAL;
-          }
-          ycov[v[i]] = 1;
+  // coverage of x (Q-task columns) and y (P-task rows); every output row has
+  // exactly one P-task writer (an atomic exchange finds a second one)
+  int64_t dup_row = -1;
+  for (int32_t s : {0, Lmax}) {
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t q = 0; q < (int64_t)stages[s].size(); ++q) {
+      const TaskB& t = stages[s][q];
+      for (auto& c : t.cols)
+        if (c.type == SIDE_X) {
+          const int64_t* v = lg.src_vals.v(c.id);
+          for (int64_t i = 0; i < c.len; ++i) __atomic_store_n(&xcov[v[i]], 1, __ATOMIC_RELAXED);
         }
-      }
+      for (auto& rw : t.rows)
+        if (rw.type == SIDE_Y) {
+          const int64_t* v = lg.obs_vals.v(rw.id);
+          for (int64_t i = 0; i < rw.len; ++i)
+            if (__atomic_exchange_n(&ycov[v[i]], (uint8_t)1, __ATOMIC_RELAXED))
+              __atomic_store_n(&dup_row, v[i], __ATOMIC_RELAXED);
+        }
+    }
+  }
+  if (dup_row >= 0) {
+    set_error("pack: output row %lld written by two P tasks", (long long)dup_row);
+    return BF_EINVAL;
   }
   plog.mark("pack: emit tasks/maps");
   // forward launch lists by task shape (kernels in bf_matvec.cu)
