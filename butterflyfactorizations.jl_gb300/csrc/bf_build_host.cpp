@@ -13,6 +13,7 @@
 #include <cstring>
 #include <stdexcept>
 #include <unordered_map>
+#include <parallel/algorithm>
 
 #include "bf_build.h"
 #include "bf_surrogate.h"
@@ -48,12 +49,35 @@ struct SkelRef {
   int64_t slot = -1;  // level slot holding this skeleton's values (pack_plan wiring)
 };
 
-// the skeleton map K (bfassembly.jl:76-77): (bf, source node, observer node) -> skeleton
+// the skeleton map K (bfassembly.jl:76-77): (bf, source node, observer node) ->
+// skeleton.  Sharded by far pair, so that a round of updates is applied by
+// one thread per shard, each in update order (lookups see the same values as
+// with serial updates).
 struct KMap {
-  FlatMap<SkelRef> m;
+  static constexpr int NS = 256;
+  FlatMap<SkelRef> m[NS];
+  static int shard(int32_t bf) { return (int)(((uint32_t)bf * 2654435761u) >> 24); }
   static uint64_t lo(const KKey& k) { return ((uint64_t)k.s << 32) | (uint64_t)(uint32_t)k.o; }
-  const SkelRef& at(const KKey& k) const { return m.at((uint64_t)(uint32_t)k.bf, lo(k)); }
-  void set(const KKey& k, const SkelRef& v) { m.put((uint64_t)(uint32_t)k.bf, lo(k), v); }
+  const SkelRef& at(const KKey& k) const {
+    return m[shard(k.bf)].at((uint64_t)(uint32_t)k.bf, lo(k));
+  }
+  void set_all(const std::vector<std::pair<KKey, SkelRef>>& upd) {
+    const int64_t n = (int64_t)upd.size();
+    std::vector<int64_t> beg(NS + 1, 0), idx(n);
+    for (int64_t i = 0; i < n; ++i) ++beg[shard(upd[i].first.bf) + 1];
+    for (int s = 0; s < NS; ++s) beg[s + 1] += beg[s];
+    std::vector<int64_t> pos(beg.begin(), beg.end() - 1);
+    for (int64_t i = 0; i < n; ++i) idx[pos[shard(upd[i].first.bf)]++] = i;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int s = 0; s < NS; ++s) {
+      FlatMap<SkelRef>& ms = m[s];
+      ms.reserve(ms.count + (size_t)(beg[s + 1] - beg[s]));
+      for (int64_t j = beg[s]; j < beg[s + 1]; ++j) {
+        const auto& u = upd[idx[j]];
+        ms.put((uint64_t)(uint32_t)u.first.bf, lo(u.first), u.second);
+      }
+    }
+  }
 };
 
 struct BFState {
@@ -283,21 +307,50 @@ int Builder::run_compressions(std::vector<HTask>& tasks, const std::vector<int32
       pending.push_back(work[pos++]);
     }
     while (!pending.empty()) {
-      // larger shared-memory needs last, so each QR launch covers one size bucket
-      std::stable_sort(pending.begin(), pending.end(), [&](int64_t a, int64_t b) {
-        return (int64_t)tasks[a].rows * tasks[a].n_cols < (int64_t)tasks[b].rows * tasks[b].n_cols;
-      });
-      int64_t np = (int64_t)pending.size();
-      ct.assign(np, CTask{});
-      int64_t zo = 0, ro = 0, po = 0;
+      // larger shared-memory needs last, so each QR launch covers one size
+      // bucket: sizes ascending, ties in pending order (a stable sort, done as
+      // a parallel sort of (size, position) keys)
+      const int64_t np = (int64_t)pending.size();
+      {
+        std::vector<std::pair<int64_t, int64_t>> key(np);
+#pragma omp parallel for schedule(static)
+        for (int64_t q = 0; q < np; ++q) {
+          const HTask& t = tasks[pending[q]];
+          key[q] = {(int64_t)t.rows * t.n_cols, q};
+        }
+        __gnu_parallel::sort(key.begin(), key.end());
+        std::vector<int64_t> sorted(np);
+#pragma omp parallel for schedule(static)
+        for (int64_t q = 0; q < np; ++q) sorted[q] = pending[key[q].second];
+        pending.swap(sorted);
+      }
+      // offsets of every compression's sample, rows and column permutation
+      // (sizes gathered in parallel, serial prefix sums), then the records
+      std::vector<int64_t> zoff(np + 1, 0), roff(np + 1, 0), poff(np + 1, 0);
+#pragma omp parallel for schedule(static)
       for (int64_t q = 0; q < np; ++q) {
         const HTask& t = tasks[pending[q]];
-        CTask& c = ct[q];
-        c.z_off = zo;
-        c.rows_off = ro;
+        zoff[q + 1] = (int64_t)t.rows * t.n_cols;
+        roff[q + 1] = t.rows;
+        poff[q + 1] = t.n_cols;
+      }
+      for (int64_t q = 0; q < np; ++q) {
+        zoff[q + 1] += zoff[q];
+        roff[q + 1] += roff[q];
+        poff[q + 1] += poff[q];
+      }
+      const int64_t zo = zoff[np], ro = roff[np], po = poff[np];
+      n_entries_ += zo;
+      ct.resize(np);
+#pragma omp parallel for schedule(static)
+      for (int64_t q = 0; q < np; ++q) {
+        const HTask& t = tasks[pending[q]];
+        CTask c{};
+        c.z_off = zoff[q];
+        c.rows_off = roff[q];
         c.cols_off = t.cols_off;
         c.obs_begin = t.obs_begin;
-        c.perm_off = po;
+        c.perm_off = poff[q];
         c.t_off = -1;
         c.skel_off = 0;
         c.key = t.key;
@@ -306,10 +359,7 @@ int Builder::run_compressions(std::vector<HTask>& tasks, const std::vector<int32
         c.n_rows = t.rows;
         c.n_cols = t.n_cols;
         c.rank = 0;
-        zo += (int64_t)t.rows * t.n_cols;
-        ro += t.rows;
-        po += t.n_cols;
-        n_entries_ += (int64_t)t.rows * t.n_cols;
+        ct[q] = c;
       }
       BF_TRY(dev_reserve(d_ctask_, ctask_cap_, np));
       BF_TRY(dev_reserve(d_Z_, z_cap_, zo));
@@ -349,50 +399,69 @@ int Builder::run_compressions(std::vector<HTask>& tasks, const std::vector<int32
       // adaptive decisions (compressors.jl:134-151)
       next.clear();
       done.clear();
-      int64_t tsum = 0, ssum = 0;
-      int max_rank = 0;
+      std::vector<uint8_t> retry(np, 0);
+      int64_t n_fb = 0, n_rt = 0;
+#pragma omp parallel for schedule(static) reduction(+ : n_fb, n_rt)
       for (int64_t q = 0; q < np; ++q) {
         HTask& t = tasks[pending[q]];
         t.rank = ct[q].rank;
-        bool retry = opts_.adaptive && t.rank > (int32_t)std::floor(0.8 * t.rows) &&
-                     t.rows < t.n_obs;
-        if (retry) {
+        if (opts_.adaptive && t.rank > (int32_t)std::floor(0.8 * t.rows) && t.rows < t.n_obs) {
           int32_t nr = t.rows * 2;
           if (t.seeded && !t.fell_back) {
             // the surrogate under-predicted: fall back to the oversampling
             // estimator's count (or the doubled sample, if larger)
             nr = std::max(nr, t.n_est);
             t.fell_back = 1;
-            ++n_fallback_;
+            ++n_fb;
           }
           t.rows = std::min(nr, t.n_obs);
           t.retries++;
-          ++n_retry_;
-          next.push_back(pending[q]);
-        } else {
-          done.push_back(q);
-          tsum += (int64_t)t.rank * t.n_cols;
-          ssum += t.rank;
-          max_rank = std::max(max_rank, t.rank);
+          ++n_rt;
+          retry[q] = 1;
         }
       }
+      n_fallback_ += n_fb;
+      n_retry_ += n_rt;
+      for (int64_t q = 0; q < np; ++q) {
+        if (retry[q])
+          next.push_back(pending[q]);
+        else
+          done.push_back(q);
+      }
       if (!done.empty()) {
+        // factor-store and skeleton offsets of the finished compressions, in
+        // their order (sizes in parallel, serial prefix sums)
+        const int64_t nd = (int64_t)done.size();
+        std::vector<int64_t> toff(nd + 1, 0), soff(nd + 1, 0);
+        int max_rank = 0;
+#pragma omp parallel for schedule(static) reduction(max : max_rank)
+        for (int64_t d = 0; d < nd; ++d) {
+          const HTask& t = tasks[pending[done[d]]];
+          toff[d + 1] = (int64_t)t.rank * t.n_cols;
+          soff[d + 1] = t.rank;
+          max_rank = std::max(max_rank, t.rank);
+        }
+        for (int64_t d = 0; d < nd; ++d) {
+          toff[d + 1] += toff[d];
+          soff[d + 1] += soff[d];
+        }
+        const int64_t tsum = toff[nd], ssum = soff[nd];
         BF_TRY(ensure_raw(raw_used_ + tsum));
         BF_TRY(dev_reserve(d_skel_, skel_cap_, std::max<int64_t>(ssum, 1)));
-        std::vector<CTask> dct;
-        dct.reserve(done.size());
-        int64_t so = 0;
-        for (int64_t q : done) {
+        std::vector<CTask> dct(nd);
+        const int64_t raw0 = raw_used_, skel0 = (int64_t)skel_.size();
+#pragma omp parallel for schedule(static)
+        for (int64_t d = 0; d < nd; ++d) {
+          const int64_t q = done[d];
           HTask& t = tasks[pending[q]];
           CTask c = ct[q];
-          c.t_off = raw_used_;
-          c.skel_off = so;
-          t.t_off = raw_used_;
-          t.skel = SkelRef{(int64_t)skel_.size() + so, t.rank};
-          raw_used_ += (int64_t)t.rank * t.n_cols;
-          so += t.rank;
-          dct.push_back(c);
+          c.t_off = raw0 + toff[d];
+          c.skel_off = soff[d];
+          t.t_off = raw0 + toff[d];
+          t.skel = SkelRef{skel0 + soff[d], t.rank};
+          dct[d] = c;
         }
+        raw_used_ = raw0 + tsum;
         // done tasks reuse the front of the CTask buffer (their Z stays in place)
         BF_TRY_CUDA(cudaMemcpyAsync(d_ctask_, dct.data(), dct.size() * sizeof(CTask),
                                     cudaMemcpyHostToDevice, st_));
@@ -459,6 +528,7 @@ int Builder::seed_rows(std::vector<HTask>& tasks) {
   if (!surrogate_ || tasks.empty()) return BF_OK;
   const int64_t n = (int64_t)tasks.size();
   std::vector<float> feat(4 * n), pred(n);
+#pragma omp parallel for schedule(static)
   for (int64_t q = 0; q < n; ++q) {
     const HTask& t = tasks[q];
     surrogate_features(to_, ts_, k_, t.stage, t.obs_node, t.src_node, t.n_obs, t.n_cols,
@@ -480,6 +550,7 @@ int Builder::seed_rows(std::vector<HTask>& tasks) {
                               cudaMemcpyDeviceToHost, st_));
   BF_TRY_CUDA(cudaStreamSynchronize(st_));
   const double margin = opts_.surrogate_margin;
+#pragma omp parallel for schedule(static)
   for (int64_t q = 0; q < n; ++q) {
     HTask& t = tasks[q];
     double r = std::exp(std::min((double)pred[q] + margin, 30.0));
@@ -687,7 +758,13 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
       lg.blocks[bb + q] = make_block(t.bf, 0, t.obs_node, t.src_node, t.obs_node, t.src_node,
                                      t.rank, t.n_cols, 0, t.t_off, t.rank, -1, t.skel.slot);
     }
-    for (const HTask& t : tasks) K_.set(KKey{t.bf, t.src_node, t.obs_node}, t.skel);
+    {
+      std::vector<std::pair<KKey, SkelRef>> upd(nt);
+#pragma omp parallel for schedule(static)
+      for (int64_t q = 0; q < nt; ++q)
+        upd[q] = {KKey{tasks[q].bf, tasks[q].src_node, tasks[q].obs_node}, tasks[q].skel};
+      K_.set_all(upd);
+    }
     log_tasks(tasks);
   }
   blog.mark("build: Q stage");
@@ -864,9 +941,10 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
       }
     }
     if (failed) throw std::out_of_range("skeleton map lookup");
+    blog.mark("build: R level emit blocks");
     log_tasks(tasks);
-    blog.mark("build: R level emit");
-    for (auto& u : upd) K_.set(u.first, u.second);
+    blog.mark("build: R level rank records");
+    K_.set_all(upd);
     blog.mark("build: R level skeleton map");
   }
   // ---- P stage (bfassembly.jl:186-197)

@@ -60,6 +60,7 @@ struct DSU {
 }  // namespace
 
 int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
+  PhaseLog plog;
   plan = Plan();
   plan.n_rows = lg.n_rows;
   plan.n_cols = lg.n_cols;
@@ -75,34 +76,66 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
     return BF_EINVAL;
   }
   // ---- per-BF depth (number of levels = #R + 1)
+  // (parallel over blocks; an error names the first offending block, as a
+  // serial scan would)
   std::vector<int32_t> nlev(n_bf, 1);
+  int64_t bad_bf = nb, bad_size = nb;
+#pragma omp parallel for schedule(static) reduction(min : bad_bf, bad_size)
   for (int64_t b = 0; b < nb; ++b) {
     const LBlock& k = B[b];
     if (k.bf < 0 || k.bf >= n_bf) {
-      set_error("pack: block %lld has bf id %d out of range", (long long)b, k.bf);
-      return BF_EINVAL;
+      bad_bf = std::min(bad_bf, b);
+      continue;
     }
-    if (k.stage > 0) nlev[k.bf] = std::max(nlev[k.bf], k.stage + 1);
-    if (!k.ident && (k.rows < 0 || k.cols < 0)) {
-      set_error("pack: block %lld has negative size", (long long)b);
-      return BF_EINVAL;
+    if (k.stage > 0) {
+      const int32_t v = k.stage + 1;
+      int32_t cur = __atomic_load_n(&nlev[k.bf], __ATOMIC_RELAXED);
+      while (cur < v && !__atomic_compare_exchange_n(&nlev[k.bf], &cur, v, false,
+                                                     __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {
+      }
     }
+    if (!k.ident && (k.rows < 0 || k.cols < 0)) bad_size = std::min(bad_size, b);
+  }
+  if (bad_bf < nb && bad_bf <= bad_size) {
+    set_error("pack: block %lld has bf id %d out of range", (long long)bad_bf, B[bad_bf].bf);
+    return BF_EINVAL;
+  }
+  if (bad_size < nb) {
+    set_error("pack: block %lld has negative size", (long long)bad_size);
+    return BF_EINVAL;
   }
   int32_t Lmax = *std::max_element(nlev.begin(), nlev.end());
   // block order by (stage rank, original order): Q, R1, R2, ..., P -- a
-  // counting sort over the Lmax + 1 stage ranks (stable)
+  // counting sort over the Lmax + 1 stage ranks, stable: contiguous block
+  // ranges count and scatter in parallel, each range in order
   std::vector<int64_t> order(nb);
   std::vector<int64_t> sbeg(Lmax + 2, 0);  // order[sbeg[r] .. sbeg[r+1]): stage rank r
   {
     auto srank = [&](const LBlock& k) { return k.stage < 0 ? Lmax : k.stage; };
-    std::vector<int64_t> cnt(Lmax + 2, 0);
-    for (int64_t b = 0; b < nb; ++b) ++cnt[srank(B[b]) + 1];
-    for (int32_t r = 0; r <= Lmax; ++r) cnt[r + 1] += cnt[r];
-    sbeg = cnt;
-    for (int64_t b = 0; b < nb; ++b) order[cnt[srank(B[b])]++] = b;
+    const int64_t C = std::max<int64_t>(1, std::min<int64_t>(nb / 65536, 256));
+    const int R = Lmax + 1;
+    std::vector<int64_t> cnt((size_t)C * R, 0);
+#pragma omp parallel for schedule(static)
+    for (int64_t c = 0; c < C; ++c)
+      for (int64_t b = nb * c / C; b < nb * (c + 1) / C; ++b) ++cnt[c * R + srank(B[b])];
+    for (int r = 0; r < R; ++r) {
+      int64_t tot = 0;
+      for (int64_t c = 0; c < C; ++c) tot += cnt[c * R + r];
+      sbeg[r + 1] = sbeg[r] + tot;
+    }
+    for (int r = 0; r < R; ++r) {  // cnt -> scatter position of range c, rank r
+      int64_t p = sbeg[r];
+      for (int64_t c = 0; c < C; ++c) {
+        const int64_t n = cnt[c * R + r];
+        cnt[c * R + r] = p;
+        p += n;
+      }
+    }
+#pragma omp parallel for schedule(static)
+    for (int64_t c = 0; c < C; ++c)
+      for (int64_t b = nb * c / C; b < nb * (c + 1) / C; ++b) order[cnt[c * R + srank(B[b])]++] = b;
   }
-
-  PhaseLog plog;
+  plog.mark("pack: checks + block order");
   // ---- slot wiring (bfstructs.jl:107-143)
   // key (bf, level, o, s) packed exactly into 128 bits (node ids < 2^32)
   FlatMap<int64_t> slot_of;
@@ -358,11 +391,19 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
   }
   plog.mark("pack: P tasks");
   // big tasks first inside each launch (longest-processing-time order)
-  // (GCC's parallel-mode stable sort: the result of a stable sort is unique)
-  for (auto& st : stages)
-    __gnu_parallel::stable_sort(st.begin(), st.end(), [](const TaskB& a, const TaskB& b) {
-      return a.M * a.n > b.M * b.n;
-    });
+  // (a parallel sort of (size, position) keys, so ties keep their order as in
+  // a stable sort; then the tasks move into place)
+  for (auto& st : stages) {
+    const int64_t n = (int64_t)st.size();
+    std::vector<std::pair<int64_t, int64_t>> key(n);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) key[i] = {-(st[i].M * st[i].n), i};
+    __gnu_parallel::sort(key.begin(), key.end());
+    std::vector<TaskB> sorted(n);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) sorted[i] = std::move(st[key[i].second]);
+    st.swap(sorted);
+  }
 
   plog.mark("pack: LPT sort");
   // ---- workspace layout: [x space | y space | slots in reader order]
@@ -633,6 +674,14 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
   plan.alg_bytes_fwd = (int64_t)plan.fac_bytes * plan.block_entries +
                        16 * (lg.n_rows + lg.n_cols + 2 * slot_total);
   plog.mark("pack: class lists + totals");
+  // tens of millions of small task vectors: freed by all threads
+  for (auto& st : stages) {
+#pragma omp parallel for schedule(static, 4096)
+    for (int64_t i = 0; i < (int64_t)st.size(); ++i) st[i] = TaskB();
+  }
+  stages.clear();
+  stages.shrink_to_fit();
+  plog.mark("pack: free task lists");
   return BF_OK;
 }
 
