@@ -105,6 +105,30 @@ __device__ __forceinline__ double cabs2(float2 a) {
   return (double)a.x * a.x + (double)a.y * a.y;
 }
 
+// Sum of |c[i]|^2 over i = i0, i0+step, ... < i1, as an FP64 value.  Every
+// square of an FP32 value is split exactly into a float pair by the FMA and
+// added with TwoSum into a float-float accumulator on the FP32 pipes (relative
+// error ~ count * 2^-48); the pair is rounded to FP64 once.  This keeps the
+// column norms FP64-accurate without one FP64 operation per entry, which on
+// GB300's narrow FP64 pipe bounded the QR kernel.
+__device__ __forceinline__ void ff_add(float& sh, float& sl, float b) {
+  const float s = __fadd_rn(sh, b);
+  const float v = __fsub_rn(s, sh);
+  sl = __fadd_rn(sl, __fadd_rn(__fsub_rn(sh, __fsub_rn(s, v)), __fsub_rn(b, v)));
+  sh = s;
+}
+__device__ __forceinline__ double sumsq(const float2* __restrict__ c, int i0, int i1, int step) {
+  float sh = 0.f, sl = 0.f;
+  for (int i = i0; i < i1; i += step) {
+    const float2 a = c[i];
+    const float p = __fmul_rn(a.x, a.x), q = __fmul_rn(a.y, a.y);
+    ff_add(sh, sl, p);
+    ff_add(sh, sl, q);
+    sl = __fadd_rn(sl, __fadd_rn(__fmaf_rn(a.x, a.x, -p), __fmaf_rn(a.y, a.y, -q)));
+  }
+  return (double)sh + (double)sl;
+}
+
 template <int NT>
 __device__ __forceinline__ void block_argmax(double& v, int& idx, double* rv, int* ri) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -182,8 +206,7 @@ __global__ void __launch_bounds__(QR_NT) qr_kernel(CTask* __restrict__ tasks,
   __syncthreads();
   for (int j = tid; j < m; j += QR_NT) {
     perm[j] = j;
-    double s = 0.0;
-    for (int i = 0; i < n; ++i) s += cabs2(Z[i + (long long)j * ld]);
+    const double s = sumsq(Z + (long long)j * ld, 0, n, 1);
     nrm[j] = s;
     orig[j] = s;
   }
@@ -226,8 +249,7 @@ __global__ void __launch_bounds__(QR_NT) qr_kernel(CTask* __restrict__ tasks,
       }
     }
     __syncthreads();
-    double xs = 0.0;
-    for (int i = k + 1 + tid; i < n; i += QR_NT) xs += cabs2(Z[i + (long long)k * ld]);
+    const double xs = sumsq(Z + (long long)k * ld, k + 1 + tid, n, QR_NT);
     double xn2 = block_sum<QR_NT>(xs, rv);
     if (tid == 0) {
       float2 alpha = Z[k + (long long)k * ld];
@@ -272,19 +294,21 @@ __global__ void __launch_bounds__(QR_NT) qr_kernel(CTask* __restrict__ tasks,
       }
     }
     __syncthreads();
-    // norm downdate (xLAQP2), in FP64
+    // norm downdate (xLAQP2), in FP64.  The norms here are squared, so
+    // xLAQP2's nrm*max(1 - |z|^2/nrm, 0) is max(nrm - |z|^2, 0) and its
+    // cancellation test max(1 - |z|^2/nrm, 0)*nrm/orig <= tol3z reads
+    // max(nrm - |z|^2, 0) <= tol3z*orig: the same quantities without the two
+    // FP64 divisions per column and step, which bound this kernel on the FP64
+    // pipe.
     for (int j = k + 1 + tid; j < m; j += QR_NT) {
       if (nrm[j] > 0.0) {
-        double t = 1.0 - cabs2(Z[k + (long long)j * ld]) / nrm[j];
-        t = fmax(t, 0.0);
-        double t2 = t * (nrm[j] / orig[j]);
-        if (t2 <= tol3z) {
-          double s = 0.0;
-          for (int i = k + 1; i < n; ++i) s += cabs2(Z[i + (long long)j * ld]);
+        const double t = fmax(nrm[j] - cabs2(Z[k + (long long)j * ld]), 0.0);
+        if (t <= tol3z * orig[j]) {
+          const double s = sumsq(Z + (long long)j * ld, k + 1, n, 1);
           nrm[j] = s;
           orig[j] = s;
         } else {
-          nrm[j] *= t;
+          nrm[j] = t;
         }
       }
     }
