@@ -129,48 +129,6 @@ __device__ __forceinline__ double sumsq(const float2* __restrict__ c, int i0, in
   return (double)sh + (double)sl;
 }
 
-template <int NT>
-__device__ __forceinline__ void block_argmax(double& v, int& idx, double* rv, int* ri) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    double ov = __shfl_xor_sync(0xffffffffu, v, o);
-    int oi = __shfl_xor_sync(0xffffffffu, idx, o);
-    if (ov > v || (ov == v && oi < idx)) {
-      v = ov;
-      idx = oi;
-    }
-  }
-  if (lane == 0) {
-    rv[wid] = v;
-    ri[wid] = idx;
-  }
-  __syncthreads();
-  v = rv[0];
-  idx = ri[0];
-#pragma unroll
-  for (int w = 1; w < NT / 32; ++w)
-    if (rv[w] > v || (rv[w] == v && ri[w] < idx)) {
-      v = rv[w];
-      idx = ri[w];
-    }
-  __syncthreads();
-}
-
-template <int NT>
-__device__ __forceinline__ double block_sum(double v, double* rv) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  if (lane == 0) rv[wid] = v;
-  __syncthreads();
-  double s = 0.0;
-#pragma unroll
-  for (int w = 0; w < NT / 32; ++w) s += rv[w];
-  __syncthreads();
-  return s;
-}
-
 // Column-pivoted Householder QR of one sampled block, stopped once the largest
 // remaining column norm is <= eps * |R_00| (the truncation of LowRankApprox.pqr
 // with rtol = eps, compressors.jl:129).  LAPACK xGEQP3/xLAQP2 conventions:
@@ -216,20 +174,53 @@ __global__ void __launch_bounds__(QR_NT) qr_kernel(CTask* __restrict__ tasks,
   double r00 = 0.0;
   int rank = kmax;
   for (int k = 0; k < kmax; ++k) {
-    double bv = -1.0;
+    // pivot: the largest remaining FP64 column norm, lowest index on ties.
+    // Non-negative doubles (and the -1 sentinel) order like their bit
+    // patterns read as signed 64-bit integers, so the search runs on the
+    // integer pipes; thread 0 alone combines the warps, takes the square root
+    // and decides the truncation (r00 lives in thread 0).
+    long long bv = __double_as_longlong(-1.0);
     int bi = m;
-    for (int j = k + tid; j < m; j += QR_NT)
-      if (nrm[j] > bv) {
-        bv = nrm[j];
+    for (int j = k + tid; j < m; j += QR_NT) {
+      const long long v = __double_as_longlong(nrm[j]);
+      if (v > bv) {
+        bv = v;
         bi = j;
       }
-    block_argmax<QR_NT>(bv, bi, rv, ri);
-    double pn = sqrt(fmax(bv, 0.0));
-    if (k == 0) r00 = pn;
-    if (r00 == 0.0 || pn <= task.eps * r00) {
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long ov = __shfl_xor_sync(0xffffffffu, bv, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > bv || (ov == bv && oi < bi)) {
+        bv = ov;
+        bi = oi;
+      }
+    }
+    if ((tid & 31) == 0) {
+      rv[tid >> 5] = __longlong_as_double(bv);
+      ri[tid >> 5] = bi;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      for (int w = 1; w < QR_NT / 32; ++w) {
+        const long long ov = __double_as_longlong(rv[w]);
+        if (ov > bv || (ov == bv && ri[w] < bi)) {
+          bv = ov;
+          bi = ri[w];
+        }
+      }
+      const double pn = sqrt(fmax(__longlong_as_double(bv), 0.0));
+      if (k == 0) r00 = pn;
+      ri[QR_NT / 32] = bi;
+      ri[QR_NT / 32 + 1] = (r00 == 0.0 || pn <= task.eps * r00) ? 1 : 0;
+    }
+    __syncthreads();
+    if (ri[QR_NT / 32 + 1]) {
       rank = k;
       break;
     }
+    bi = ri[QR_NT / 32];
     if (bi != k) {
       for (int i = tid; i < n; i += QR_NT) {
         float2 a = Z[i + (long long)k * ld];
@@ -249,22 +240,27 @@ __global__ void __launch_bounds__(QR_NT) qr_kernel(CTask* __restrict__ tasks,
       }
     }
     __syncthreads();
-    const double xs = sumsq(Z + (long long)k * ld, k + 1 + tid, n, QR_NT);
-    double xn2 = block_sum<QR_NT>(xs, rv);
-    if (tid == 0) {
-      float2 alpha = Z[k + (long long)k * ld];
-      if (xn2 == 0.0 && alpha.y == 0.0f) {
-        sc[0] = make_float2(0.f, 0.f);  // tau = 0, H = I
-        sc[1] = make_float2(0.f, 0.f);
-      } else {
-        double ar = alpha.x, ai = alpha.y;
-        double beta = -copysign(sqrt(ar * ar + ai * ai + xn2), ar);
-        float2 tau = make_float2((float)((beta - ar) / beta), (float)(-ai / beta));
-        double dr = ar - beta, di = ai;  // scale = 1 / (alpha - beta)
-        double den = dr * dr + di * di;
-        sc[0] = tau;
-        sc[1] = make_float2((float)(dr / den), (float)(-di / den));
-        Z[k + (long long)k * ld] = make_float2((float)beta, 0.f);
+    // Householder reflector of column k: warp 0 sums the squares below the
+    // diagonal, its lane 0 forms tau and the scale
+    if (tid < 32) {
+      double xn2 = sumsq(Z + (long long)k * ld, k + 1 + tid, n, 32);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) xn2 += __shfl_xor_sync(0xffffffffu, xn2, o);
+      if (tid == 0) {
+        float2 alpha = Z[k + (long long)k * ld];
+        if (xn2 == 0.0 && alpha.y == 0.0f) {
+          sc[0] = make_float2(0.f, 0.f);  // tau = 0, H = I
+          sc[1] = make_float2(0.f, 0.f);
+        } else {
+          double ar = alpha.x, ai = alpha.y;
+          double beta = -copysign(sqrt(ar * ar + ai * ai + xn2), ar);
+          float2 tau = make_float2((float)((beta - ar) / beta), (float)(-ai / beta));
+          double dr = ar - beta, di = ai;  // scale = 1 / (alpha - beta)
+          double den = dr * dr + di * di;
+          sc[0] = tau;
+          sc[1] = make_float2((float)(dr / den), (float)(-di / den));
+          Z[k + (long long)k * ld] = make_float2((float)beta, 0.f);
+        }
       }
     }
     __syncthreads();
