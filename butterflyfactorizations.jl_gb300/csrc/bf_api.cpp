@@ -174,6 +174,7 @@ int bf_import_factors(bf_ctx_t ctx, const bf_factor_desc* d, bf_op_t* out) {
     k.cols = k.ident ? 0 : d->cols[b];
     k.raw_off = d->data_off[b];
     k.raw_ld = std::max(k.rows, 1);
+    k.in_slot = k.out_slot = -1;  // wiring derived by pack_plan from the routing keys
     if (!k.ident) {
       if (k.rows < 0 || k.cols < 0 || k.raw_off < 0) {
         delete h;

@@ -614,6 +614,7 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
   // slot ids follow the skeleton map: every new skeleton (or identity copy) of
   // a level gets a fresh slot, blocks read the slot of the skeleton they use
   std::vector<int64_t> slot_len;
+  std::vector<BlockVec> stage_blocks;  // blocks of each stage, joined at the end
   auto make_block = [](int32_t bf, int32_t stage, int64_t oo, int64_t so, int64_t oi, int64_t si,
                        int32_t rows, int32_t cols, int8_t ident, int64_t raw_off, int32_t ld,
                        int64_t in_slot, int64_t out_slot) {
@@ -747,16 +748,16 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
     join(parts, tasks, pool, nullptr, nullptr);
     BF_TRY(run_compressions(tasks, pool));
     const int64_t nt = (int64_t)tasks.size();
-    const int64_t sb = (int64_t)slot_len.size(), bb = (int64_t)lg.blocks.size();
+    const int64_t sb = (int64_t)slot_len.size();
     slot_len.resize(sb + nt);
-    lg.blocks.resize(bb + nt);
+    BlockVec& blk = stage_blocks.emplace_back(nt);
 #pragma omp parallel for schedule(static)
     for (int64_t q = 0; q < nt; ++q) {
       HTask& t = tasks[q];
       t.skel.slot = sb + q;
       slot_len[sb + q] = t.rank;
-      lg.blocks[bb + q] = make_block(t.bf, 0, t.obs_node, t.src_node, t.obs_node, t.src_node,
-                                     t.rank, t.n_cols, 0, t.t_off, t.rank, -1, t.skel.slot);
+      blk[q] = make_block(t.bf, 0, t.obs_node, t.src_node, t.obs_node, t.src_node, t.rank,
+                          t.n_cols, 0, t.t_off, t.rank, -1, t.skel.slot);
     }
     {
       std::vector<std::pair<KKey, SkelRef>> upd(nt);
@@ -898,9 +899,9 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
       boff[q + 1] = (it.kind == 0 && it.split_svert >= 0) ? ts_.n_child[it.split_svert] : 1;
     }
     for (int64_t q = 0; q < ni; ++q) boff[q + 1] += boff[q];
-    const int64_t sb = (int64_t)slot_len.size(), bb = (int64_t)lg.blocks.size();
+    const int64_t sb = (int64_t)slot_len.size();
     slot_len.resize(sb + ni);
-    lg.blocks.resize(bb + boff[ni]);
+    BlockVec& blk = stage_blocks.emplace_back(boff[ni]);
     std::vector<std::pair<KKey, SkelRef>> upd(ni);
     std::atomic<int> failed{0};
 #pragma omp parallel for schedule(static)
@@ -908,29 +909,29 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
       try {
         const Item& it = items[q];
         const int64_t slot = sb + q;
-        int64_t b = bb + boff[q];
+        int64_t b = boff[q];
         if (it.kind == 1) {
           SkelRef out = it.copy;
           out.slot = slot;
           slot_len[slot] = it.copy.len;
-          lg.blocks[b] = make_block(it.bf, l, it.oo, it.so, it.oi, it.si, 0, 0, 1, 0, 1,
-                                    it.copy.slot, slot);
+          blk[b] = make_block(it.bf, l, it.oo, it.so, it.oi, it.si, 0, 0, 1, 0, 1, it.copy.slot,
+                              slot);
           upd[q] = {KKey{it.bf, it.upd_s, it.upd_o}, out};
         } else {
           HTask& t = tasks[it.task];
           t.skel.slot = slot;
           slot_len[slot] = t.rank;
           if (it.split_svert < 0) {
-            lg.blocks[b] = make_block(it.bf, l, it.oo, it.so, it.oi, it.si, t.rank, t.n_cols, 0,
-                                      t.t_off, t.rank, K_.at(KKey{it.bf, it.si, it.oi}).slot, slot);
+            blk[b] = make_block(it.bf, l, it.oo, it.so, it.oi, it.si, t.rank, t.n_cols, 0, t.t_off,
+                                t.rank, K_.at(KKey{it.bf, it.si, it.oi}).slot, slot);
           } else {
             int64_t c0 = 0;
             const int64_t Sv = it.split_svert;
             for (int32_t ch = 0; ch < ts_.n_child[Sv]; ++ch) {
               const int64_t Sc = ts_.first_child[Sv] + ch;
               const SkelRef& in = K_.at(KKey{it.bf, Sc, it.oi});
-              lg.blocks[b++] = make_block(it.bf, l, it.oo, it.so, it.oi, Sc, t.rank, in.len, 0,
-                                          t.t_off + c0 * t.rank, t.rank, in.slot, slot);
+              blk[b++] = make_block(it.bf, l, it.oo, it.so, it.oi, Sc, t.rank, in.len, 0,
+                                    t.t_off + c0 * t.rank, t.rank, in.slot, slot);
               c0 += in.len;
             }
           }
@@ -976,13 +977,25 @@ int Builder::run(const double* obs_xyz, int64_t n_obs, const double* src_xyz, in
     join(parts, tasks, pool, nullptr, &in_slots);
     BF_TRY(run_dense(tasks, pool));
     const int64_t nt = (int64_t)tasks.size();
-    const int64_t bb = (int64_t)lg.blocks.size();
-    lg.blocks.resize(bb + nt);
+    BlockVec& blk = stage_blocks.emplace_back(nt);
 #pragma omp parallel for schedule(static)
     for (int64_t q = 0; q < nt; ++q) {
       const HTask& t = tasks[q];
-      lg.blocks[bb + q] = make_block(t.bf, -1, t.obs_node, t.src_node, t.obs_node, t.src_node,
-                                     t.n_obs, t.n_cols, 0, t.t_off, t.n_obs, in_slots[q], -1);
+      blk[q] = make_block(t.bf, -1, t.obs_node, t.src_node, t.obs_node, t.src_node, t.n_obs,
+                          t.n_cols, 0, t.t_off, t.n_obs, in_slots[q], -1);
+    }
+  }
+  {  // the stages' blocks, in stage order, into one array (parallel copy)
+    int64_t tot = 0;
+    for (const BlockVec& v : stage_blocks) tot += (int64_t)v.size();
+    lg.blocks.resize(tot);
+    int64_t off = 0;
+    for (BlockVec& v : stage_blocks) {
+      const int64_t n = (int64_t)v.size();
+#pragma omp parallel for schedule(static)
+      for (int64_t q = 0; q < n; ++q) lg.blocks[off + q] = v[q];
+      off += n;
+      BlockVec().swap(v);
     }
   }
   lg.slot_len = std::move(slot_len);

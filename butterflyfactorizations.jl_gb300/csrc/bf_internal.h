@@ -7,8 +7,10 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
+#include <memory>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "bfgpu.h"
@@ -131,6 +133,8 @@ bool is_far(const Tree& ts, const Tree& to, int64_t snode, int64_t onode, double
 // ---------------------------------------------------------------- logical factors
 // One reference ButterflyBlock (bfstructs.jl:21-29) whose matrix lives in a raw
 // device array (column-major, leading dimension raw_ld).
+// A plain struct (no member initialisers): every producer sets every field,
+// and vectors of blocks are grown without a serial initialisation pass.
 struct LBlock {
   int32_t bf;
   int32_t stage;  // 0 = Q, l = R level l, -1 = P
@@ -141,8 +145,31 @@ struct LBlock {
   int32_t raw_ld;
   // slot ids when the producer already knows the wiring (the GPU build);
   // -1: derived by pack_plan from the routing keys
-  int64_t in_slot = -1, out_slot = -1;
+  int64_t in_slot, out_slot;
 };
+
+// Allocator whose value-less construct() default-initialises: resize() of a
+// vector of plain structs then leaves the new elements for the caller (and the
+// first touch of their pages to the threads that fill them).
+template <typename T>
+struct DefaultInitAlloc : std::allocator<T> {
+  template <typename U>
+  struct rebind {
+    using other = DefaultInitAlloc<U>;
+  };
+  DefaultInitAlloc() = default;
+  template <typename U>
+  DefaultInitAlloc(const DefaultInitAlloc<U>&) noexcept {}
+  template <typename U>
+  void construct(U* p) noexcept {
+    ::new (static_cast<void*>(p)) U;
+  }
+  template <typename U, typename... Args>
+  void construct(U* p, Args&&... args) {
+    ::new (static_cast<void*>(p)) U(std::forward<Args>(args)...);
+  }
+};
+using BlockVec = std::vector<LBlock, DefaultInitAlloc<LBlock>>;
 
 // node -> values map (CSR), 0-based point indices
 struct ValuesMap {
@@ -154,7 +181,7 @@ struct ValuesMap {
 struct Logical {
   int64_t n_rows = 0, n_cols = 0;
   int32_t n_bf = 0;
-  std::vector<LBlock> blocks;
+  BlockVec blocks;
   ValuesMap obs_vals, src_vals;
   // with slot ids in the blocks: the length of every slot (else empty)
   std::vector<int64_t> slot_len;
