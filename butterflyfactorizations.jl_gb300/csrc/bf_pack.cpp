@@ -160,14 +160,18 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
     // wiring supplied by the producer (the GPU build): slot ids and lengths
     slot_len = lg.slot_len;
     const int64_t ns = (int64_t)slot_len.size();
+    int64_t bad = nb;
+#pragma omp parallel for schedule(static) reduction(min : bad)
     for (int64_t b = 0; b < nb; ++b) {
       in_slot[b] = B[b].in_slot;
       out_slot[b] = B[b].out_slot;
       if (in_slot[b] >= ns || out_slot[b] >= ns ||
-          (B[b].stage != 0 && in_slot[b] < 0) || (B[b].stage >= 0 && out_slot[b] < 0)) {
-        set_error("pack: block %lld has invalid slot ids", (long long)b);
-        return BF_EINVAL;
-      }
+          (B[b].stage != 0 && in_slot[b] < 0) || (B[b].stage >= 0 && out_slot[b] < 0))
+        bad = std::min(bad, b);
+    }
+    if (bad < nb) {
+      set_error("pack: block %lld has invalid slot ids", (long long)bad);
+      return BF_EINVAL;
     }
   } else
   for (int64_t b : order) {
@@ -250,9 +254,9 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
   std::vector<std::vector<TaskB>> stages(Lmax + 1);
   {  // Q stage: group by source node (node ids validated above)
     std::vector<int64_t> gid(lg.src_vals.ptr.size(), -1);
-    for (int64_t b : order) {
+    for (int64_t i = sbeg[0]; i < sbeg[1]; ++i) {
+      const int64_t b = order[i];
       const LBlock& k = B[b];
-      if (k.stage != 0) continue;
       if (gid[k.si] < 0) {
         gid[k.si] = (int64_t)stages[0].size();
         TaskB t;
@@ -370,9 +374,9 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
   plog.mark("pack: R tasks");
   {  // P stage: group by observer node (node ids validated above)
     std::vector<int64_t> gid(lg.obs_vals.ptr.size(), -1);
-    for (int64_t b : order) {
+    for (int64_t i = sbeg[Lmax]; i < sbeg[Lmax + 1]; ++i) {  // stage rank Lmax: P blocks
+      const int64_t b = order[i];
       const LBlock& k = B[b];
-      if (k.stage >= 0) continue;
       if (gid[k.oo] < 0) {
         gid[k.oo] = (int64_t)stages[Lmax].size();
         TaskB t;
