@@ -264,6 +264,23 @@ __global__ void __launch_bounds__(MX_THREADS) mx_level_kernel(
     const int o0 = un.y, no = un.z;
     const int nib_total = ADJ ? Mb : nb;
     const int nchunks = (nib_total + MX_IB - 1) / MX_IB;
+    // thread j = right-hand side j gathers the input entries of a chunk; the
+    // next chunk's entries are requested before the current chunk is split
+    // and multiplied, so two chunks of gathers are in flight
+    float2 vnext[MX_IC];
+    auto gather = [&](float2 (&v)[MX_IC], int chunk) {
+      const int kb = chunk * MX_IB, knb = min(MX_IB, nib_total - kb);
+#pragma unroll
+      for (int c = 0; c < MX_IC; ++c) {
+        const int e = kb * 8 + c;
+        v[c] = make_float2(0.f, 0.f);
+        if (c < knb * 8 && e < nin) {
+          const int64_t slot = in_base >= 0 ? (int64_t)in_base + e : (int64_t)in_map[e];
+          v[c] = ws[(size_t)slot * MX_R + tid];
+        }
+      }
+    };
+    if (nchunks > 0) gather(vnext, 0);
 
     for (int ch = 0; ch < nchunks; ++ch, ++it) {
       const int st = it & 1, use = it >> 1;
@@ -295,19 +312,13 @@ __global__ void __launch_bounds__(MX_THREADS) mx_level_kernel(
         }
         last_copy_use[st] = use;
       }
-      // gather + split the inputs: thread j = right-hand side j
+      // split the gathered inputs into BF16 hi/lo planes: thread j = right-hand side j
       {
         const int j = tid;
         float2 v[MX_IC];
 #pragma unroll
-        for (int c = 0; c < MX_IC; ++c) {
-          const int e = k0 * 8 + c;
-          v[c] = make_float2(0.f, 0.f);
-          if (c < kn * 8 && e < nin) {
-            const int64_t slot = in_base >= 0 ? (int64_t)in_base + e : (int64_t)in_map[e];
-            v[c] = ws[(size_t)slot * MX_R + j];
-          }
-        }
+        for (int c = 0; c < MX_IC; ++c) v[c] = vnext[c];
+        if (ch + 1 < nchunks) gather(vnext, ch + 1);
         uint8_t* xg = smem + st * MX_STAGE + (j >> 3) * 128 + (j & 7) * 16;
 #pragma unroll
         for (int g = 0; g < MX_IC / 4; ++g) {

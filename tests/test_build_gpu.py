@@ -99,3 +99,20 @@ def test_far_operator_build_matches_dense(ctx):
     bfs = export_to_oracle(op.export_blocks(), ot, ot)
     fop = O.FarOperator(bfs, far, n, n)
     assert relerr(op @ x, O.far_matvec(fop, x)) <= 1e-12
+
+
+def test_build_is_deterministic(ctx):
+    """The host side of the build runs in parallel (far-pair chunks, sharded
+    skeleton map, parallel packing); every step reproduces the serial order, so
+    two builds of one operator give the same ranks and bit-identical products."""
+    n = 16384
+    pts = G.fibonacci_sphere(n)
+    tr = bfgpu.Tree.build(pts, max_points=32)
+    k = G.wavenumber(n, 4 * math.pi)
+    a = bfgpu.PetrovGalerkinBF(pts, pts, tr, tr, k, tol=TOL, ctx=ctx)
+    b = bfgpu.PetrovGalerkinBF(pts, pts, tr, tr, k, tol=TOL, ctx=ctx)
+    assert a.stats()["n_bf"] > 1000  # many far-pair chunks
+    assert np.array_equal(a.rank_log(), b.rank_log())
+    x = G.complex_gaussian(n, 5)
+    assert np.array_equal(a @ x, b @ x)
+    assert np.array_equal(a.adjoint() @ x, b.adjoint() @ x)
