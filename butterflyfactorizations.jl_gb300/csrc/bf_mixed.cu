@@ -213,7 +213,54 @@ __device__ __forceinline__ uint32_t pack_bf2(__nv_bfloat16 a, __nv_bfloat16 b) {
   return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
 }
 
-// ADJ = 0: out = rows (M), in = columns (n); ADJ = 1: the other way round.
+// One work unit (a task and a group of output blocks), ADJ = 0: out = rows
+// (M), in = columns (n); ADJ = 1: the other way round.
+struct MxUnit {
+  int64_t fo;  // first byte of the task's BF16 blocks
+  const int32_t* in_map;
+  const int32_t* out_map;
+  int Mb, nb, nin, nout, in_base, out_base, o0, no, nib_total, nchunks;
+};
+
+template <int ADJ>
+__device__ __forceinline__ MxUnit mx_unit(int u, const int4* __restrict__ units,
+                                          const DTask* __restrict__ tasks,
+                                          const int64_t* __restrict__ moff,
+                                          const int32_t* __restrict__ maps) {
+  const int4 un = units[u];
+  const DTask t = tasks[un.x];
+  MxUnit d;
+  d.fo = moff[un.x];
+  d.Mb = (t.M + 7) >> 3;
+  d.nb = (t.n + 7) >> 3;
+  d.nin = ADJ ? t.M : t.n;
+  d.nout = ADJ ? t.n : t.M;
+  d.in_base = ADJ ? t.rbase : t.cbase;
+  d.in_map = maps + (ADJ ? t.rmap_off : t.cmap_off);
+  d.out_base = ADJ ? t.cbase : t.rbase;
+  d.out_map = maps + (ADJ ? t.cmap_off : t.rmap_off);
+  d.o0 = un.y;
+  d.no = un.z;
+  d.nib_total = ADJ ? d.Mb : d.nb;
+  d.nchunks = (d.nib_total + MX_IB - 1) / MX_IB;
+  return d;
+}
+
+// the input entries of one chunk for right-hand side j
+__device__ __forceinline__ void mx_gather(const MxUnit& d, const float2* __restrict__ ws,
+                                          float2 (&v)[MX_IC], int chunk, int j) {
+  const int kb = chunk * MX_IB, knb = min(MX_IB, d.nib_total - kb);
+#pragma unroll
+  for (int c = 0; c < MX_IC; ++c) {
+    const int e = kb * 8 + c;
+    v[c] = make_float2(0.f, 0.f);
+    if (c < knb * 8 && e < d.nin) {
+      const int64_t slot = d.in_base >= 0 ? (int64_t)d.in_base + e : (int64_t)d.in_map[e];
+      v[c] = ws[(size_t)slot * MX_R + j];
+    }
+  }
+}
+
 template <int ADJ>
 __global__ void __launch_bounds__(MX_THREADS) mx_level_kernel(
     const int4* __restrict__ units, int n_units, int* __restrict__ counter,
@@ -223,8 +270,8 @@ __global__ void __launch_bounds__(MX_THREADS) mx_level_kernel(
   extern __shared__ __align__(128) uint8_t smem[];
   uint64_t* bars = (uint64_t*)(smem + MX_NST * MX_STAGE);  // fbar[2], mbar[2]
   uint32_t* tslot = (uint32_t*)(bars + 4);
-  volatile int* s_unit = (volatile int*)(tslot + 1);
-  volatile int* s_dead = s_unit + 1;
+  volatile int* s_unit = (volatile int*)(tslot + 1);  // two slots
+  volatile int* s_dead = s_unit + 2;
   const int tid = threadIdx.x, warp = tid >> 5;
   const uint32_t sbase = smem_u32(smem);
   const uint32_t fbar0 = smem_u32(bars), mbar0 = smem_u32(bars + 2);
@@ -247,40 +294,28 @@ __global__ void __launch_bounds__(MX_THREADS) mx_level_kernel(
   int last_copy_use[MX_NST] = {-1, -1}, last_commit_use[MX_NST] = {-1, -1};
   int it = 0;  // global chunk counter of this CTA
 
+  // Thread j = right-hand side j gathers the input entries of a chunk.  The
+  // next chunk's entries are requested before the current chunk is split and
+  // multiplied, and the next unit (claimed when the current one starts) has
+  // its descriptor and first chunk requested before the current unit's
+  // epilogue waits for its MMAs.  The unit index alternates between two
+  // shared slots, so a claim never overwrites an index not yet read.
+  if (tid == 0) s_unit[0] = atomicAdd(counter, 1);
+  __syncthreads();
+  int u = s_unit[0], uslot = 0;
+  MxUnit cur{};
+  float2 vnext[MX_IC];
+  if (u < n_units) {
+    cur = mx_unit<ADJ>(u, units, tasks, moff, maps);
+    if (cur.nchunks > 0) mx_gather(cur, ws, vnext, 0, tid);
+  }
   for (;;) {
-    if (tid == 0) *s_unit = atomicAdd(counter, 1);
-    __syncthreads();
-    const int u = *s_unit;
     if (u >= n_units || *s_dead) break;
-    const int4 un = units[u];
-    const DTask t = tasks[un.x];
-    const int64_t fo = moff[un.x];
-    const int Mb = (t.M + 7) >> 3, nb = (t.n + 7) >> 3;
-    const int nin = ADJ ? t.M : t.n, nout = ADJ ? t.n : t.M;
-    const int in_base = ADJ ? t.rbase : t.cbase;
-    const int32_t* __restrict__ in_map = maps + (ADJ ? t.rmap_off : t.cmap_off);
-    const int out_base = ADJ ? t.cbase : t.rbase;
-    const int32_t* __restrict__ out_map = maps + (ADJ ? t.cmap_off : t.rmap_off);
-    const int o0 = un.y, no = un.z;
-    const int nib_total = ADJ ? Mb : nb;
-    const int nchunks = (nib_total + MX_IB - 1) / MX_IB;
-    // thread j = right-hand side j gathers the input entries of a chunk; the
-    // next chunk's entries are requested before the current chunk is split
-    // and multiplied, so two chunks of gathers are in flight
-    float2 vnext[MX_IC];
-    auto gather = [&](float2 (&v)[MX_IC], int chunk) {
-      const int kb = chunk * MX_IB, knb = min(MX_IB, nib_total - kb);
-#pragma unroll
-      for (int c = 0; c < MX_IC; ++c) {
-        const int e = kb * 8 + c;
-        v[c] = make_float2(0.f, 0.f);
-        if (c < knb * 8 && e < nin) {
-          const int64_t slot = in_base >= 0 ? (int64_t)in_base + e : (int64_t)in_map[e];
-          v[c] = ws[(size_t)slot * MX_R + tid];
-        }
-      }
-    };
-    if (nchunks > 0) gather(vnext, 0);
+    if (tid == 0) s_unit[uslot ^ 1] = atomicAdd(counter, 1);
+    const int64_t fo = cur.fo;
+    const int Mb = cur.Mb, nout = cur.nout, out_base = cur.out_base;
+    const int32_t* __restrict__ out_map = cur.out_map;
+    const int o0 = cur.o0, no = cur.no, nib_total = cur.nib_total, nchunks = cur.nchunks;
 
     for (int ch = 0; ch < nchunks; ++ch, ++it) {
       const int st = it & 1, use = it >> 1;
@@ -318,7 +353,7 @@ __global__ void __launch_bounds__(MX_THREADS) mx_level_kernel(
         float2 v[MX_IC];
 #pragma unroll
         for (int c = 0; c < MX_IC; ++c) v[c] = vnext[c];
-        if (ch + 1 < nchunks) gather(vnext, ch + 1);
+        if (ch + 1 < nchunks) mx_gather(cur, ws, vnext, ch + 1, tid);
         uint8_t* xg = smem + st * MX_STAGE + (j >> 3) * 128 + (j & 7) * 16;
 #pragma unroll
         for (int g = 0; g < MX_IC / 4; ++g) {
@@ -385,6 +420,14 @@ __global__ void __launch_bounds__(MX_THREADS) mx_level_kernel(
     }
     __syncthreads();
     if (*s_dead) break;
+    // the next unit's descriptor and first chunk are requested before the wait
+    // below (inputs and outputs of a level are disjoint slots)
+    const int u_next = s_unit[uslot ^ 1];
+    MxUnit nxt{};
+    if (u_next < n_units) {
+      nxt = mx_unit<ADJ>(u_next, units, tasks, moff, maps);
+      if (nxt.nchunks > 0) mx_gather(nxt, ws, vnext, 0, tid);
+    }
     // epilogue: every MMA of the unit is done once the last commit has landed
     {
       const int last = it - 1;
@@ -410,6 +453,9 @@ __global__ void __launch_bounds__(MX_THREADS) mx_level_kernel(
     tc_fence_before();
     __syncthreads();
     if (*s_dead) break;
+    cur = nxt;
+    u = u_next;
+    uslot ^= 1;
   }
 
   // drain: let this CTA's own copies and MMAs finish before freeing tensor memory
