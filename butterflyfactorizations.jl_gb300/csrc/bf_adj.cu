@@ -33,23 +33,31 @@ __device__ __forceinline__ float4 vin(const DTask& t, const int32_t* __restrict_
 
 __device__ __forceinline__ int rg_of(int M) { return M <= 8 ? 2 : (M <= 32 ? 4 : 8); }
 
-// Partial sums of columns c = c0 + cg + CG*u (u < cpl) over rows
-// [r_begin, r_end) for this lane; summed over the RG lanes of the column group
-// on return (every lane of the group holds the group total).
+constexpr int ADJ_VS = 128;  // staged input entries per warp
+
+// input entries of rows [r, r + len) into the warp's staging buffer
+__device__ __forceinline__ void adj_stage(const DTask& t, const int32_t* __restrict__ rmap,
+                                          const float4* __restrict__ ws, float4* __restrict__ vs,
+                                          int r, int len) {
+  for (int i = threadIdx.x & 31; i < len; i += 32) vs[i] = vin(t, rmap, ws, r + i);
+}
+
+// Adds, for this lane, the partial sums of columns c = c0 + cg + CG*u (u < cpl)
+// over rows [r_begin, r_end) whose input entries are staged at vs[r - vbase].
+// The input entries are gathered once into shared memory (adj_stage), so the
+// row walk waits on the factor loads only, not on a routing-map lookup and a
+// dependent workspace load per row.
 template <bool CONJ, int RG, typename FT>
-__device__ __forceinline__ void adj_pass(const DTask& t, const FT* __restrict__ A,
-                                         const float4* __restrict__ ws,
-                                         const int32_t* __restrict__ rmap, int r_begin, int r_end,
-                                         int c0, int cpl, float4 acc[ADJ_CPL]) {
+__device__ __forceinline__ void adj_accum(const DTask& t, const FT* __restrict__ A,
+                                          const float4* __restrict__ vs, int vbase, int r_begin,
+                                          int r_end, int c0, int cpl, float4 acc[ADJ_CPL]) {
   constexpr int CG = 32 / RG;
   const int lane = threadIdx.x & 31;
   const int rg = lane % RG, cg = lane / RG;
   const int M = t.M, n = t.n;
-#pragma unroll
-  for (int u = 0; u < ADJ_CPL; ++u) acc[u] = make_float4(0.f, 0.f, 0.f, 0.f);
   const FT* __restrict__ Ab = A + t.a_off;
   for (int r = r_begin + rg; r < r_end; r += RG) {
-    const float4 v = vin(t, rmap, ws, r);
+    const float4 v = vs[r - vbase];
     FT a[ADJ_CPL];
 #pragma unroll
     for (int u = 0; u < ADJ_CPL; ++u) {
@@ -66,11 +74,40 @@ __device__ __forceinline__ void adj_pass(const DTask& t, const FT* __restrict__ 
       }
     }
   }
+}
+
+// the RG partial sums of each column meet (every lane of the group holds the total)
+template <int RG>
+__device__ __forceinline__ void adj_reduce(float4 acc[ADJ_CPL], int cpl) {
 #pragma unroll
   for (int m = 1; m < RG; m <<= 1)
 #pragma unroll
     for (int u = 0; u < ADJ_CPL; ++u)
       if (u < cpl) cdf_add(acc[u], shfl_xor4(acc[u], m));
+}
+
+// rows [r0, r1) of column pass c0 for this warp: already staged (staged =
+// true, at vs[r - r0]) or staged here in chunks of ADJ_VS rows
+template <bool CONJ, int RG, typename FT>
+__device__ __forceinline__ void adj_rows(const DTask& t, const FT* __restrict__ A,
+                                         const int32_t* __restrict__ rmap,
+                                         const float4* __restrict__ ws, float4* __restrict__ vs,
+                                         bool staged, int r0, int r1, int c0, int cpl,
+                                         float4 acc[ADJ_CPL]) {
+#pragma unroll
+  for (int u = 0; u < ADJ_CPL; ++u) acc[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (staged) {
+    adj_accum<CONJ, RG, FT>(t, A, vs, r0, r0, r1, c0, cpl, acc);
+  } else {
+    for (int rc = r0; rc < r1; rc += ADJ_VS) {  // chunk starts stay multiples of RG
+      const int len = min(ADJ_VS, r1 - rc);
+      __syncwarp();
+      adj_stage(t, rmap, ws, vs, rc, len);
+      __syncwarp();
+      adj_accum<CONJ, RG, FT>(t, A, vs, rc, rc, rc + len, c0, cpl, acc);
+    }
+  }
+  adj_reduce<RG>(acc, cpl);
 }
 
 __device__ __forceinline__ void write_out(const DTask& t, const int32_t* __restrict__ cmap,
@@ -84,7 +121,7 @@ __device__ __forceinline__ void write_out(const DTask& t, const int32_t* __restr
 template <bool CONJ, int RG, typename FT>
 __device__ void adj_task_warp(const DTask& t, const FT* __restrict__ A,
                               const int32_t* __restrict__ maps, float4* __restrict__ ws,
-                              int pass_begin, int pass_step) {
+                              float4* __restrict__ vs, int pass_begin, int pass_step) {
   constexpr int CG = 32 / RG;
   const int lane = threadIdx.x & 31;
   const int rg = lane % RG, cg = lane / RG;
@@ -92,9 +129,15 @@ __device__ void adj_task_warp(const DTask& t, const FT* __restrict__ A,
   const int32_t* __restrict__ cmap = maps + t.cmap_off;
   const int cpl = min(ADJ_CPL, (t.n + CG - 1) / CG);
   const int per_pass = CG * cpl;
+  // the task's input entries are staged once when they fit
+  const bool staged = t.M <= ADJ_VS;
+  if (staged) {
+    adj_stage(t, rmap, ws, vs, 0, t.M);
+    __syncwarp();
+  }
   float4 acc[ADJ_CPL];
   for (int c0 = pass_begin * per_pass; c0 < t.n; c0 += pass_step * per_pass) {
-    adj_pass<CONJ, RG, FT>(t, A, ws, rmap, 0, t.M, c0, cpl, acc);
+    adj_rows<CONJ, RG, FT>(t, A, rmap, ws, vs, staged, 0, t.M, c0, cpl, acc);
     if (rg == 0) {
 #pragma unroll
       for (int u = 0; u < ADJ_CPL; ++u) {
@@ -103,6 +146,7 @@ __device__ void adj_task_warp(const DTask& t, const FT* __restrict__ A,
       }
     }
   }
+  __syncwarp();
 }
 
 // warp per task (small tasks)
@@ -113,13 +157,15 @@ __global__ void __launch_bounds__(256) adj_warp_kernel(const int32_t* __restrict
                                                        const FT* __restrict__ A,
                                                        const int32_t* __restrict__ maps,
                                                        float4* __restrict__ ws) {
+  __shared__ float4 vsm[8][ADJ_VS];
   const int ti = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (ti >= n_tasks) return;
   const DTask t = tasks[tlist[ti]];
+  float4* vs = vsm[threadIdx.x >> 5];
   switch (rg_of(t.M)) {
-    case 2: adj_task_warp<CONJ, 2, FT>(t, A, maps, ws, 0, 1); break;
-    case 4: adj_task_warp<CONJ, 4, FT>(t, A, maps, ws, 0, 1); break;
-    default: adj_task_warp<CONJ, 8, FT>(t, A, maps, ws, 0, 1); break;
+    case 2: adj_task_warp<CONJ, 2, FT>(t, A, maps, ws, vs, 0, 1); break;
+    case 4: adj_task_warp<CONJ, 4, FT>(t, A, maps, ws, vs, 0, 1); break;
+    default: adj_task_warp<CONJ, 8, FT>(t, A, maps, ws, vs, 0, 1); break;
   }
 }
 
@@ -130,16 +176,17 @@ __global__ void __launch_bounds__(256) adj_wide_kernel(const int32_t* __restrict
                                                        const FT* __restrict__ A,
                                                        const int32_t* __restrict__ maps,
                                                        float4* __restrict__ ws) {
+  __shared__ float4 vsm[8][ADJ_VS];
   const DTask t = tasks[tlist[blockIdx.x]];
   const int w = threadIdx.x >> 5;
   switch (rg_of(t.M)) {
-    case 2: adj_task_warp<CONJ, 2, FT>(t, A, maps, ws, w, 8); break;
-    case 4: adj_task_warp<CONJ, 4, FT>(t, A, maps, ws, w, 8); break;
-    default: adj_task_warp<CONJ, 8, FT>(t, A, maps, ws, w, 8); break;
+    case 2: adj_task_warp<CONJ, 2, FT>(t, A, maps, ws, vsm[w], w, 8); break;
+    case 4: adj_task_warp<CONJ, 4, FT>(t, A, maps, ws, vsm[w], w, 8); break;
+    default: adj_task_warp<CONJ, 8, FT>(t, A, maps, ws, vsm[w], w, 8); break;
   }
 }
 
-// CTA per tall task (M > 32): the 8 warps split the rows; per column pass the
+// CTA per tall task (M > 128): the 8 warps split the rows; per column pass the
 // warp partials meet in shared memory.
 template <bool CONJ, typename FT>
 __global__ void __launch_bounds__(256) adj_tall_kernel(const int32_t* __restrict__ tlist,
@@ -149,6 +196,7 @@ __global__ void __launch_bounds__(256) adj_tall_kernel(const int32_t* __restrict
                                                        float4* __restrict__ ws) {
   constexpr int RG = 8, CG = 4;
   __shared__ float4 red[8][CG * ADJ_CPL];
+  __shared__ float4 vsm[8][ADJ_VS];
   const DTask t = tasks[tlist[blockIdx.x]];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int rg = lane % RG, cg = lane / RG;
@@ -159,9 +207,15 @@ __global__ void __launch_bounds__(256) adj_tall_kernel(const int32_t* __restrict
   // row split in multiples of RG so that row groups stay aligned
   const int rows_per_warp = ((t.M + 8 * RG - 1) / (8 * RG)) * RG;
   const int r0 = min(t.M, w * rows_per_warp), r1 = min(t.M, r0 + rows_per_warp);
+  // a warp's rows are staged once when they fit
+  const bool staged = r1 - r0 <= ADJ_VS;
+  if (staged) {
+    adj_stage(t, rmap, ws, vsm[w], r0, r1 - r0);
+    __syncwarp();
+  }
   float4 acc[ADJ_CPL];
   for (int c0 = 0; c0 < t.n; c0 += per_pass) {
-    adj_pass<CONJ, RG, FT>(t, A, ws, rmap, r0, r1, c0, cpl, acc);
+    adj_rows<CONJ, RG, FT>(t, A, rmap, ws, vsm[w], staged, r0, r1, c0, cpl, acc);
     if (rg == 0) {
 #pragma unroll
       for (int u = 0; u < ADJ_CPL; ++u)
