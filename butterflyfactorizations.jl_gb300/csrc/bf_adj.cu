@@ -56,6 +56,8 @@ __device__ __forceinline__ void adj_accum(const DTask& t, const FT* __restrict__
   const int rg = lane % RG, cg = lane / RG;
   const int M = t.M, n = t.n;
   const FT* __restrict__ Ab = A + t.a_off;
+  // (two row steps per iteration were measured slower: the extra registers
+  // cost more occupancy than the extra loads in flight gained)
   for (int r = r_begin + rg; r < r_end; r += RG) {
     const float4 v = vs[r - vbase];
     FT a[ADJ_CPL];
