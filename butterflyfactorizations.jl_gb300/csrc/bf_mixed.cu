@@ -23,12 +23,14 @@
 //     stored blocks as MN-major B operands (Ahat^T is the real form of A^H);
 //     the transpose conjugates inputs and outputs on top of that.
 //
-// Pipeline per CTA (4 warps, 3 CTAs per SM): two stages of shared memory,
-// each one input chunk (16 entries x 128 right-hand sides, hi and lo) plus the
-// matching factor blocks.  Thread 0 issues the bulk copies of the factor
-// blocks and the MMAs; all 128 threads gather and split the inputs and run
-// the epilogue (thread j owns right-hand side j = tensor-memory lane j).  The
-// MMAs of one chunk overlap the gathering of the next.  Every wait is bounded.
+// Pipeline per CTA (4 warps, 4 CTAs per SM, 128 tensor-memory columns each):
+// two stages of shared memory, each one input chunk (8 entries x 128
+// right-hand sides, hi and lo) plus the matching factor blocks.  Thread 0
+// issues the bulk copies of the factor blocks and the MMAs; all 128 threads
+// gather and split the inputs and run the epilogue (thread j owns right-hand
+// side j = tensor-memory lane j).  The MMAs of one chunk overlap the gathering
+// of the next; the gathers run one chunk and one unit ahead (gathering two
+// chunks ahead was measured slower).  Every wait is bounded.
 #include <cuda_bf16.h>
 
 #include <algorithm>
