@@ -17,6 +17,8 @@
 // list read backwards with rows and columns swapped.
 #include <algorithm>
 #include <cstring>
+#include <memory>
+#include <memory_resource>
 #include <numeric>
 #include <parallel/algorithm>
 
@@ -36,12 +38,17 @@ struct Member {
   int32_t row_off, col_off;
   int32_t ident_n;
 };
+// The tens of millions of R-level tasks take their arrays from per-chunk
+// monotonic arenas (a pointer bump per allocation, one release per arena), so
+// that building and dropping them does not go through the general allocator.
 struct TaskB {
   int32_t stage;
   int32_t kind;
-  std::vector<Side> rows, cols;
-  std::vector<Member> mats;
+  std::pmr::vector<Side> rows, cols;
+  std::pmr::vector<Member> mats;
   int64_t M = 0, n = 0;
+  TaskB() = default;
+  explicit TaskB(std::pmr::memory_resource* r) : rows(r), cols(r), mats(r) {}
 };
 
 struct DSU {
@@ -251,6 +258,7 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
 
   plog.mark("pack: order + slot wiring");
   // ---- tasks
+  std::vector<std::unique_ptr<std::pmr::monotonic_buffer_resource>> arenas;  // outlive stages
   std::vector<std::vector<TaskB>> stages(Lmax + 1);
   {  // Q stage: group by source node (node ids validated above)
     std::vector<int64_t> gid(lg.src_vals.ptr.size(), -1);
@@ -311,10 +319,14 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
     }
     const int64_t nc = (int64_t)cut.size() - 1;
     std::vector<std::vector<TaskB>> part(nc);
+    const size_t a0 = arenas.size();
+    for (int64_t c = 0; c < nc; ++c)
+      arenas.push_back(std::make_unique<std::pmr::monotonic_buffer_resource>());
 #pragma omp parallel for schedule(dynamic, 1)
     for (int64_t c = 0; c < nc; ++c) {
       DSU d;
       std::vector<TaskB>& out = part[c];
+      std::pmr::memory_resource* arena = arenas[a0 + c].get();
       auto idx = [&](int64_t slot) {
         if (slot_lvl[slot] == l) return slot_dsu[slot];
         int64_t i = (int64_t)d.p.size();
@@ -332,7 +344,7 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
         const int64_t b = order[i];
         const LBlock& k = B[b];
         if (k.ident) {
-          TaskB t;
+          TaskB t(arena);
           t.stage = l;
           t.kind = TASK_COPY;
           int64_t len = slot_len[in_slot[b]];
@@ -345,7 +357,7 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
         int64_t root = d.find(idx(in_slot[b]));
         if (comp[root] < 0) {
           comp[root] = (int64_t)out.size();
-          TaskB t;
+          TaskB t(arena);
           t.stage = l;
           t.kind = TASK_DENSE;
           out.push_back(std::move(t));
@@ -397,16 +409,22 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
   // big tasks first inside each launch (longest-processing-time order)
   // (a parallel sort of (size, position) keys, so ties keep their order as in
   // a stable sort; then the tasks move into place)
-  for (auto& st : stages) {
+  // lpt[s] lists the tasks of stage s in that order; the tasks stay in place
+  std::vector<std::vector<int64_t>> lpt(Lmax + 1), lpos(Lmax + 1);  // order and its inverse
+  for (int32_t s = 0; s <= Lmax; ++s) {
+    const std::vector<TaskB>& st = stages[s];
     const int64_t n = (int64_t)st.size();
     std::vector<std::pair<int64_t, int64_t>> key(n);
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i) key[i] = {-(st[i].M * st[i].n), i};
     __gnu_parallel::sort(key.begin(), key.end());
-    std::vector<TaskB> sorted(n);
+    lpt[s].resize(n);
+    lpos[s].resize(n);
 #pragma omp parallel for schedule(static)
-    for (int64_t i = 0; i < n; ++i) sorted[i] = std::move(st[key[i].second]);
-    st.swap(sorted);
+    for (int64_t i = 0; i < n; ++i) {
+      lpt[s][i] = key[i].second;
+      lpos[s][key[i].second] = i;
+    }
   }
 
   plog.mark("pack: LPT sort");
@@ -415,13 +433,54 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
   plan.yg_off = lg.n_cols;
   int64_t ws = lg.n_cols + lg.n_rows;
   std::vector<int64_t> slot_off(n_slots, -1);
-  for (int32_t s = 1; s <= Lmax; ++s)
-    for (auto& t : stages[s])
-      for (auto& c : t.cols)
-        if (c.type == SIDE_SLOT && slot_off[c.id] < 0) {
-          slot_off[c.id] = ws;
-          ws += c.len;
+  {
+    // When every slot is read by exactly one task (the case for the GPU
+    // build), the reader-order layout is a prefix sum over the tasks' column
+    // sizes and is assigned in parallel; otherwise one serial first-appearance
+    // pass gives the same definition.
+    std::vector<uint8_t> readers(n_slots, 0);
+    int shared_slot = 0;
+    for (int32_t s = 1; s <= Lmax; ++s) {
+#pragma omp parallel for schedule(dynamic, 1024) reduction(| : shared_slot)
+      for (int64_t q = 0; q < (int64_t)lpt[s].size(); ++q)
+        for (auto& c : stages[s][lpt[s][q]].cols)
+          if (c.type == SIDE_SLOT && __atomic_exchange_n(&readers[c.id], (uint8_t)1, __ATOMIC_RELAXED))
+            shared_slot = 1;
+    }
+    if (!shared_slot) {
+      for (int32_t s = 1; s <= Lmax; ++s) {
+        const int64_t n = (int64_t)lpt[s].size();
+        std::vector<int64_t> base(n + 1, 0);
+#pragma omp parallel for schedule(static)
+        for (int64_t q = 0; q < n; ++q) {
+          int64_t tot = 0;
+          for (auto& c : stages[s][lpt[s][q]].cols)
+            if (c.type == SIDE_SLOT) tot += c.len;
+          base[q + 1] = tot;
         }
+        base[0] = ws;
+        for (int64_t q = 0; q < n; ++q) base[q + 1] += base[q];
+#pragma omp parallel for schedule(static)
+        for (int64_t q = 0; q < n; ++q) {
+          int64_t o = base[q];
+          for (auto& c : stages[s][lpt[s][q]].cols)
+            if (c.type == SIDE_SLOT) {
+              slot_off[c.id] = o;
+              o += c.len;
+            }
+        }
+        ws = base[n];
+      }
+    } else {
+      for (int32_t s = 1; s <= Lmax; ++s)
+        for (int64_t i : lpt[s])
+          for (auto& c : stages[s][i].cols)
+            if (c.type == SIDE_SLOT && slot_off[c.id] < 0) {
+              slot_off[c.id] = ws;
+              ws += c.len;
+            }
+    }
+  }
   for (int64_t s = 0; s < n_slots; ++s)
     if (slot_off[s] < 0) {
       slot_off[s] = ws;
@@ -439,15 +498,15 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
   std::vector<int64_t> xpos(lg.n_cols, -1), ypos(lg.n_rows, -1);
   {
     int64_t nx = 0, ny = 0;
-    for (auto& t : stages[0])
-      for (auto& c : t.cols)
+    for (int64_t i : lpt[0])
+      for (auto& c : stages[0][i].cols)
         if (c.type == SIDE_X) {
           const int64_t* v = lg.src_vals.v(c.id);
           for (int64_t i = 0; i < c.len; ++i)
             if (xpos[v[i]] < 0) xpos[v[i]] = nx++;
         }
-    for (auto& t : stages[Lmax])
-      for (auto& r : t.rows)
+    for (int64_t i : lpt[Lmax])
+      for (auto& r : stages[Lmax][i].rows)
         if (r.type == SIDE_Y) {
           const int64_t* v = lg.obs_vals.v(r.id);
           for (int64_t i = 0; i < r.len; ++i)
@@ -489,7 +548,8 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
   for (int32_t s = 0; s <= Lmax; ++s) {
     const int64_t base = plan.stage_begin[s];
 #pragma omp parallel for schedule(static) reduction(| : too_large)
-    for (int64_t i = 0; i < (int64_t)stages[s].size(); ++i) {
+    for (int64_t i = 0; i < (int64_t)stages[s].size(); ++i) {  // storage order
+      const int64_t q = lpos[s][i];
       const TaskB& t = stages[s][i];
       if (t.M > INT32_MAX || t.n > INT32_MAX) too_large = 1;
       // counts for now; turned into offsets below
@@ -502,7 +562,7 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
           if (rr > 0 && cc > 0) ++r.seg_off;
         }
       }
-      all[base + i] = r;
+      all[base + q] = r;
     }
   }
   if (too_large) {
@@ -529,9 +589,18 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
   plan.tasks.resize(all.size());
   std::vector<int64_t> sbytes(Lmax + 1, 0);
   int64_t block_entries = 0, max_rank = 0;
+  // tasks are visited in storage order (sequential reads of the task lists);
+  // each is written at its launch-order position q
+  std::vector<int64_t> qpos(all.size());
+  for (int32_t s = 0; s <= Lmax; ++s) {
+    const int64_t base = plan.stage_begin[s];
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)stages[s].size(); ++i) qpos[base + i] = base + lpos[s][i];
+  }
 #pragma omp parallel for schedule(dynamic, 512) reduction(+ : block_entries) \
     reduction(max : max_rank)
-  for (int64_t q = 0; q < (int64_t)all.size(); ++q) {
+  for (int64_t g = 0; g < (int64_t)all.size(); ++g) {
+    const int64_t q = qpos[g];
     const TRef& r = all[q];
     const TaskB& t = stages[r.s][r.i];
     int64_t tb = 16 * (t.M + t.n);
@@ -678,13 +747,11 @@ int pack_plan(const Logical& lg, Plan& plan, int fac_bytes) {
   plan.alg_bytes_fwd = (int64_t)plan.fac_bytes * plan.block_entries +
                        16 * (lg.n_rows + lg.n_cols + 2 * slot_total);
   plog.mark("pack: class lists + totals");
-  // tens of millions of small task vectors: freed by all threads
-  for (auto& st : stages) {
-#pragma omp parallel for schedule(static, 4096)
-    for (int64_t i = 0; i < (int64_t)st.size(); ++i) st[i] = TaskB();
-  }
+  // the R tasks' arrays live in the arenas: dropping them releases a few
+  // large buffers, not one allocation per array
   stages.clear();
   stages.shrink_to_fit();
+  arenas.clear();
   plog.mark("pack: free task lists");
   return BF_OK;
 }
