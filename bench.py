@@ -533,6 +533,10 @@ def run_mixed(args, w, stream, world):
                 "d2h_bytes_per_step": 16 * n * nr},
         "roofline": {"bound": "hbm", "achieved": ach_gbs, "peak": hbm, "unit": "GB/s",
                      "frac": ach_gbs / hbm, "peak_source": f"{hbm_kind} hbm_gbs",
+                     "traffic": scaled_traffic("mixed", dom, len(sms), sby[dom]),
+                     "traffic_source": "ncu DRAM bytes per level at 16,384 points, scaled by "
+                                       "algorithmic bytes (profiles/dram_traffic_levels_"
+                                       "sphere16k.md)",
                      "kernel": f"mx_level_kernel, level {dom} of {len(sms)}, one 128-RHS chunk, "
                                f"{sms[dom]:.3f} ms",
                      "tensor_useful_tflops": useful_tf,
@@ -548,15 +552,23 @@ def run_mixed(args, w, stream, world):
     }
 
 
-def committed_traffic(workload):
-    """DRAM bytes per launch of the dominant stage from a committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "stage_traffic.json")
-    try:
-        with open(path) as f:
-            d = json.load(f)
-        return d.get(workload)
-    except (OSError, ValueError):
-        return None
+# DRAM bytes per level launch over the level's algorithmic bytes, by level kind,
+# measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the
+# 16,384-point sphere: profiles/dram_traffic_levels_sphere16k.md.  Traffic
+# grows with the algorithmic bytes (every factor entry and slot is moved once),
+# so a level's traffic at another size is this ratio times its algorithmic
+# bytes.  The R ratio is the one of the largest R level.
+TRAFFIC_RATIO = {"plain": {"Q": 0.976, "R": 0.991, "P": 1.002},
+                 "mixed": {"Q": 0.979, "R": 0.981, "P": 0.999}}
+
+
+def level_kind(dom, n_levels):
+    return "Q" if dom == 0 else "P" if dom == n_levels - 1 else "R"
+
+
+def scaled_traffic(path, dom, n_levels, alg_bytes):
+    """DRAM bytes per launch of level dom, scaled from the 16k-point capture."""
+    return int(round(TRAFFIC_RATIO[path][level_kind(dom, n_levels)] * float(alg_bytes)))
 
 
 def cpu_baseline(w, reps=3):
@@ -702,7 +714,7 @@ def run_ours(args, rank, world, local):
     dom = int(np.argmax(stage_ms))
     achieved = stage_bytes[dom] / (stage_ms[dom] * 1e-3) / 1e9
     peak, peak_kind = peaks()
-    traffic = committed_traffic(args.workload)
+    traffic = scaled_traffic("plain", dom, len(stage_ms), stage_bytes[dom])
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -726,6 +738,9 @@ def run_ours(args, rank, world, local):
                 "d2h_bytes_per_step": 16 * n},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
+                     "traffic_source": "ncu DRAM bytes per level at 16,384 points, scaled by "
+                                       "algorithmic bytes (profiles/dram_traffic_levels_"
+                                       "sphere16k.md)",
                      "kernel": f"level launch {dom} of {len(stage_ms)} "
                                f"({'Q' if dom == 0 else 'P' if dom == len(stage_ms) - 1 else 'R'}"
                                f" stage), {stage_ms[dom]:.3f} ms",
