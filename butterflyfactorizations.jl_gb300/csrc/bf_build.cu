@@ -8,6 +8,7 @@
 // the k*r range reduction of the kernel phase and for the QR column norms,
 // their downdates and the pivot choice; Householder updates, the triangular
 // solve and the factors themselves are complex FP32.
+#include <algorithm>
 #include <cfloat>
 
 #include "bf_build.h"
@@ -416,6 +417,39 @@ int launch_qr(CTask* d_tasks, int ntasks, float2* d_Z, int32_t* d_permpool, bool
     qr_kernel<true><<<ntasks, QR_NT, smem, st>>>(d_tasks, d_Z, d_permpool);
   else
     qr_kernel<false><<<ntasks, QR_NT, smem, st>>>(d_tasks, d_Z, d_permpool);
+  BF_TRY_CUDA(cudaGetLastError());
+  return BF_OK;
+}
+
+namespace {
+__global__ void ranks_kernel(const CTask* __restrict__ tasks, int n, int32_t* __restrict__ ranks) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    ranks[i] = tasks[i].rank;
+}
+__global__ void compact_done_kernel(const CTask* __restrict__ tasks, const CDone* __restrict__ done,
+                                    int n, CTask* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const CDone d = done[i];
+    CTask c = tasks[d.q];
+    c.t_off = d.t_off;
+    c.skel_off = d.skel_off;
+    out[i] = c;
+  }
+}
+}  // namespace
+
+int launch_ranks(const CTask* d_tasks, int ntasks, int32_t* d_ranks, cudaStream_t st) {
+  if (ntasks <= 0) return BF_OK;
+  ranks_kernel<<<std::min((ntasks + 255) / 256, 4096), 256, 0, st>>>(d_tasks, ntasks, d_ranks);
+  BF_TRY_CUDA(cudaGetLastError());
+  return BF_OK;
+}
+
+int launch_compact_done(const CTask* d_tasks, const CDone* d_done, int ndone, CTask* d_out,
+                        cudaStream_t st) {
+  if (ndone <= 0) return BF_OK;
+  compact_done_kernel<<<std::min((ndone + 255) / 256, 4096), 256, 0, st>>>(d_tasks, d_done, ndone,
+                                                                          d_out);
   BF_TRY_CUDA(cudaGetLastError());
   return BF_OK;
 }

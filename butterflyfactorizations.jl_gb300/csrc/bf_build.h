@@ -36,4 +36,15 @@ int launch_tsolve(const CTask* d_tasks, int ntasks, const float2* d_Z, const int
                   const int32_t* d_colpool, float2* d_raw, int32_t* d_skel, int max_rank,
                   cudaStream_t st);
 
+// ranks[i] = tasks[i].rank (only the ranks travel back to the host)
+int launch_ranks(const CTask* d_tasks, int ntasks, int32_t* d_ranks, cudaStream_t st);
+
+// A finished compression: its index in the round and its output offsets.
+struct CDone {
+  long long q, t_off, skel_off;
+};
+// out[i] = tasks[done[i].q] with the offsets of done[i] (out must not alias tasks)
+int launch_compact_done(const CTask* d_tasks, const CDone* d_done, int ndone, CTask* d_out,
+                        cudaStream_t st);
+
 }  // namespace bfg

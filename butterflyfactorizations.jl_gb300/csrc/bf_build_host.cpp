@@ -139,7 +139,8 @@ class Builder {
   ~Builder() {
     for (void* p : {(void*)d_obs_, (void*)d_src_, (void*)d_obs_perm_, (void*)d_colpool_,
                     (void*)d_ctask_, (void*)d_Z_, (void*)d_rowpool_, (void*)d_permpool_,
-                    (void*)d_skel_, (void*)d_sw_, (void*)d_sfeat_, (void*)d_sout_})
+                    (void*)d_skel_, (void*)d_sw_, (void*)d_sfeat_, (void*)d_sout_,
+                    (void*)d_ranks_, (void*)d_done_, (void*)d_ctask2_})
       if (p) cudaFree(p);
     for (cudaEvent_t e : ev_)
       if (e) cudaEventDestroy(e);
@@ -221,6 +222,12 @@ class Builder {
   int64_t perm_cap_ = 0;
   int32_t* d_skel_ = nullptr;
   int64_t skel_cap_ = 0;
+  int32_t* d_ranks_ = nullptr;  // ranks of one round
+  int64_t ranks_cap_ = 0;
+  CDone* d_done_ = nullptr;     // finished compressions of one round
+  int64_t done_cap_ = 0;
+  CTask* d_ctask2_ = nullptr;   // their records, gathered for the solve
+  int64_t ctask2_cap_ = 0;
   float2* d_raw_ = nullptr;
   int64_t raw_cap_ = 0, raw_used_ = 0;
   const Surrogate* surrogate_ = nullptr;
@@ -295,7 +302,7 @@ int Builder::run_compressions(std::vector<HTask>& tasks, const std::vector<int32
   size_t pos = 0;
   std::vector<CTask> ct;
   std::vector<int64_t> pending, next, done;
-  std::vector<int32_t> hskel;
+  std::vector<int32_t> hskel, hranks;
   while (pos < work.size()) {
     pending.clear();
     int64_t zsum = 0;
@@ -390,9 +397,13 @@ int Builder::run_compressions(std::vector<HTask>& tasks, const std::vector<int32
         BF_TRY(launch_qr(d_ctask_ + q0, (int)(q1 - q0), d_Z_, d_permpool_, fits, smax, st_));
         q0 = q1;
       }
+      // only the ranks come back (the records stay on the device)
+      BF_TRY(dev_reserve(d_ranks_, ranks_cap_, np));
+      BF_TRY(launch_ranks(d_ctask_, (int)np, d_ranks_, st_));
       if (ev_[1]) cudaEventRecord(ev_[1], st_);
-      BF_TRY_CUDA(cudaMemcpyAsync(ct.data(), d_ctask_, np * sizeof(CTask), cudaMemcpyDeviceToHost,
-                                  st_));
+      hranks.resize(np);
+      BF_TRY_CUDA(cudaMemcpyAsync(hranks.data(), d_ranks_, np * sizeof(int32_t),
+                                  cudaMemcpyDeviceToHost, st_));
       BF_TRY_CUDA(cudaStreamSynchronize(st_));
       gpu_span_end();
       ++comp_chunks_;
@@ -404,7 +415,7 @@ int Builder::run_compressions(std::vector<HTask>& tasks, const std::vector<int32
 #pragma omp parallel for schedule(static) reduction(+ : n_fb, n_rt)
       for (int64_t q = 0; q < np; ++q) {
         HTask& t = tasks[pending[q]];
-        t.rank = ct[q].rank;
+        t.rank = hranks[q];
         if (opts_.adaptive && t.rank > (int32_t)std::floor(0.8 * t.rows) && t.rows < t.n_obs) {
           int32_t nr = t.rows * 2;
           if (t.seeded && !t.fell_back) {
@@ -448,26 +459,27 @@ int Builder::run_compressions(std::vector<HTask>& tasks, const std::vector<int32
         const int64_t tsum = toff[nd], ssum = soff[nd];
         BF_TRY(ensure_raw(raw_used_ + tsum));
         BF_TRY(dev_reserve(d_skel_, skel_cap_, std::max<int64_t>(ssum, 1)));
-        std::vector<CTask> dct(nd);
+        std::vector<CDone> hdone(nd);
         const int64_t raw0 = raw_used_, skel0 = (int64_t)skel_.size();
 #pragma omp parallel for schedule(static)
         for (int64_t d = 0; d < nd; ++d) {
           const int64_t q = done[d];
           HTask& t = tasks[pending[q]];
-          CTask c = ct[q];
-          c.t_off = raw0 + toff[d];
-          c.skel_off = soff[d];
           t.t_off = raw0 + toff[d];
           t.skel = SkelRef{skel0 + soff[d], t.rank};
-          dct[d] = c;
+          hdone[d] = CDone{q, raw0 + toff[d], soff[d]};
         }
         raw_used_ = raw0 + tsum;
-        // done tasks reuse the front of the CTask buffer (their Z stays in place)
-        BF_TRY_CUDA(cudaMemcpyAsync(d_ctask_, dct.data(), dct.size() * sizeof(CTask),
+        // the finished records are gathered on the device into a second
+        // buffer with their output offsets (their sampled blocks stay in place)
+        BF_TRY(dev_reserve(d_done_, done_cap_, nd));
+        BF_TRY(dev_reserve(d_ctask2_, ctask2_cap_, nd));
+        BF_TRY_CUDA(cudaMemcpyAsync(d_done_, hdone.data(), nd * sizeof(CDone),
                                     cudaMemcpyHostToDevice, st_));
         gpu_span_begin();
-        BF_TRY(launch_tsolve(d_ctask_, (int)dct.size(), d_Z_, d_permpool_, d_colpool_, d_raw_,
-                             d_skel_, max_rank, st_));
+        BF_TRY(launch_compact_done(d_ctask_, d_done_, (int)nd, d_ctask2_, st_));
+        BF_TRY(launch_tsolve(d_ctask2_, (int)nd, d_Z_, d_permpool_, d_colpool_, d_raw_, d_skel_,
+                             max_rank, st_));
         if (ev_[1]) cudaEventRecord(ev_[1], st_);
         hskel.resize(ssum);
         if (ssum > 0)
