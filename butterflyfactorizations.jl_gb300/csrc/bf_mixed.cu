@@ -430,8 +430,10 @@ __global__ void __launch_bounds__(MX_THREADS) mx_level_kernel(
       nxt = mx_unit<ADJ>(u_next, units, tasks, moff, maps);
       if (nxt.nchunks > 0) mx_gather(nxt, ws, vnext, 0, tid);
     }
-    // epilogue: every MMA of the unit is done once the last commit has landed
-    {
+    // epilogue: every MMA of the unit is done once the last commit has landed.
+    // A unit without input entries (a task whose input slots are all empty)
+    // issued no MMA: its outputs are zero, as in the FP64 path.
+    if (nchunks > 0) {
       const int last = it - 1;
       if (!mbar_wait(mbar0 + 8 * (last & 1), (last >> 1) & 1, err)) *s_dead = 1;
     }
@@ -441,7 +443,12 @@ __global__ void __launch_bounds__(MX_THREADS) mx_level_kernel(
       const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
       for (int ob = 0; ob < no; ++ob) {
         float d[16];
-        tmem_ld16(lane_addr + ob * 16, d);
+        if (nchunks > 0) {
+          tmem_ld16(lane_addr + ob * 16, d);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 16; ++i) d[i] = 0.f;
+        }
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
           const int m = (o0 + ob) * 8 + i;
