@@ -128,3 +128,20 @@ def test_invalid_arguments_mixed(c1):
     # nrhs == 0 is a no-op
     rc = lib.bf_matvec_mixed(c1["op"]._h, 0, 0, None, 4096, None, 4096, None, None, 0, None)
     assert rc == bfgpu._lib.BF_OK
+
+
+def test_rank_zero_operator_is_zero(ctx):
+    """With tol >= 1 every compression stops at rank 0 (the first pivot already
+    meets pn <= eps*r00): every P task then has no input columns and every Q
+    task no rows.  Both paths and both directions must return exact zeros
+    (tensor-core work units without input entries issue no MMA)."""
+    n = 4096
+    pts = G.fibonacci_sphere(n)
+    tr = bfgpu.Tree.build(pts, max_points=32)
+    op = bfgpu.PetrovGalerkinBF(pts, pts, tr, tr, G.wavenumber(n, 4 * math.pi), tol=10.0,
+                                ctx=ctx)
+    assert op.stats()["n_bf"] > 0
+    X = G.complex_gaussian(n, 61, nrhs=3)
+    for view in (op, op.adjoint()):
+        assert not np.any(view.matvec(X))
+        assert not np.any(view.matvec(X, mixed=True))
