@@ -6,9 +6,9 @@
 // sequences of all operators are merged: merged level s holds level s of every
 // operator that has one.  A level is ONE persistent launch
 // (batch_level_kernel): warps take work items (operator, task, row panel) from
-// an atomic queue in longest-first order and run the FP64-accurate warp
-// routines of bf_fwd_warp.cuh for every right-hand side of the current chunk in
-// turn.  A task matrix is read from HBM once per chunk and re-read from L1/L2
+// an atomic queue in longest-first order and run FP64-accurate warp routines
+// (the bt_* routines below, same arithmetic as bf_fwd_warp.cuh) for every
+// right-hand side of the current chunk in turn.  A task matrix is read from HBM once per chunk and re-read from L1/L2
 // for the chunk's other right-hand sides.  Each operator has one workspace per
 // right-hand side of a chunk.  Chunks of `rhs_chunk` right-hand sides run one
 // after the other.
