@@ -28,8 +28,9 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import (BF_OP_C, BF_OP_N, BF_OP_T, BF_PTR_DEVICE, BF_PTR_HOST, RANK_REC_LEN, SUR_NW,
-                   BFError, BuildOpts, FactorDesc, OpStats, check, load)
+from ._lib import (BF_OP_C, BF_OP_N, BF_OP_T, BF_PTR_DEVICE, BF_PTR_HOST, BF_STORE_C32,
+                   BF_STORE_FF, RANK_REC_LEN, SUR_NW, BFError, BuildOpts, FactorDesc, OpStats,
+                   check, load)
 
 __all__ = ["Tree", "Context", "Operator", "nearandfar", "assemble_BF", "PetrovGalerkinBF",
            "import_blocks", "mul", "BFError", "load"]
@@ -241,6 +242,16 @@ class Operator:
     def __matmul__(self, x):
         return self.matvec(x)
 
+    def check(self, stream: int = 0):
+        """Synchronise ``stream`` (0: the operator's own) and raise BFError(BF_ETIMEOUT) if a
+        bounded device-side wait of an asynchronous matvec gave up since the last check."""
+        check(load().bf_op_check(self._h, C.c_void_p(stream) if stream else None),
+              "bf_op_check")
+
+    def set_wait_limit(self, polls: int):
+        """Test hook: polls of a bounded wait in the plain path (< 0: the default)."""
+        check(load().bf_op_set_wait_limit(self._h, int(polls)), "bf_op_set_wait_limit")
+
     def export_blocks(self, bf_begin: int = 0, bf_end: int | None = None,
                       as_float32: bool = False):
         """Factors of far blocks [bf_begin, bf_end) as reference-style block arrays."""
@@ -335,6 +346,36 @@ def mul(y, A: Operator, x, alpha=1.0, beta=0.0):
     return A.matvec(x, y=y, alpha=alpha, beta=beta)
 
 
+def compress_block(obs, src, obs_index, src_index, n_rows: int, key: int, k: float, eps: float,
+                   ctx: Context | None = None) -> dict:
+    """One GPU compression (``bf_compress_block``): one ``PartialQR`` call
+    (compressors.jl:81-165) on ``n_rows`` observer points sampled from
+    ``obs_index`` by the keyed bijection, against the points ``src_index``."""
+    ctx = ctx or default_context()
+    obs = np.ascontiguousarray(obs, np.float64)
+    src = np.ascontiguousarray(src, np.float64)
+    oi = np.ascontiguousarray(obs_index, np.int64)
+    si = np.ascontiguousarray(src_index, np.int64)
+    m = len(si)
+    rows = np.zeros(n_rows, np.int32)
+    Z = np.zeros((m, n_rows), np.complex64)  # column-major n_rows x m
+    rank = C.c_int32()
+    perm = np.zeros(m, np.int32)
+    kmax = min(n_rows, m)
+    skel = np.zeros(max(kmax, 1), np.int32)
+    T = np.zeros(max(kmax * m, 1), np.complex64)
+    check(load().bf_compress_block(
+        ctx._h, _p(obs, C.c_double), obs.shape[0], _p(src, C.c_double), src.shape[0],
+        _p(oi, C.c_int64), len(oi), _p(si, C.c_int64), m, int(n_rows),
+        int(key) & ((1 << 64) - 1), float(k), float(eps), _p(rows, C.c_int32),
+        Z.ctypes.data_as(C.POINTER(C.c_float)), C.byref(rank), _p(perm, C.c_int32),
+        _p(skel, C.c_int32), T.ctypes.data_as(C.POINTER(C.c_float))), "bf_compress_block")
+    r = rank.value
+    return dict(rows=rows.astype(np.int64), Z=Z.T.copy(), rank=r, perm=perm.astype(np.int64),
+                skeleton=skel[:r].astype(np.int64),
+                T=T[:r * m].reshape((m, r)).T.copy() if r > 0 else np.zeros((0, m), np.complex64))
+
+
 def import_blocks(n_rows, n_cols, bf, stage, obs_out, src_out, obs_in, src_in, rows, cols,
                   identity, data_off, data, obs_csr, src_csr, ctx: Context | None = None):
     """Upload reference-style factors (``bf_import_factors``) -> ``Operator``."""
@@ -375,7 +416,7 @@ def import_blocks(n_rows, n_cols, bf, stage, obs_out, src_out, obs_in, src_in, r
 
 
 def _build(obs, src, tree_o: Tree, tree_s: Tree, pairs, k, tol, c_tau, adaptive, seed,
-           min_samples, rank_mode, surrogate, keep_mixed, ctx):
+           min_samples, rank_mode, surrogate, keep_mixed, ctx, factor_storage=BF_STORE_C32):
     lib = load()
     ctx = ctx or default_context()
     obs = np.ascontiguousarray(obs, np.float64)
@@ -391,6 +432,7 @@ def _build(obs, src, tree_o: Tree, tree_s: Tree, pairs, k, tol, c_tau, adaptive,
     o.seed = int(seed) & ((1 << 64) - 1)
     o.rank_mode = int(rank_mode)
     o.keep_mixed = int(bool(keep_mixed))
+    o.factor_storage = int(factor_storage)
     w = None
     if surrogate is not None:
         # a bfgpu.surrogate.RankSurrogate (weights + margin) or a bare weight vector
@@ -410,18 +452,21 @@ def _build(obs, src, tree_o: Tree, tree_s: Tree, pairs, k, tol, c_tau, adaptive,
 def assemble_BF(obs, src, tree_o: Tree, tree_s: Tree, no: int, ns: int, k: float, tau: float,
                 c_tau: float = 4.0, adaptive: bool = True, seed: int = 0, min_samples: int = 10,
                 rank_mode: int = 0, surrogate=None, keep_mixed: bool = True,
-                ctx: Context | None = None) -> Operator:
-    """``assemble_BF(kernel, blktree, no, ns, k, tau)`` on the GPU (one far block)."""
+                ctx: Context | None = None, factor_storage: int = BF_STORE_C32) -> Operator:
+    """``assemble_BF(kernel, blktree, no, ns, k, tau)`` on the GPU (one far block).
+    ``factor_storage``: BF_STORE_C32 (complex FP32, 8 B per entry) or BF_STORE_FF
+    (float-float, 16 B per entry, the width of the reference's ComplexF64)."""
     return _build(obs, src, tree_o, tree_s, [(no, ns)], k, tau, c_tau, adaptive, seed,
-                  min_samples, rank_mode, surrogate, keep_mixed, ctx)
+                  min_samples, rank_mode, surrogate, keep_mixed, ctx, factor_storage)
 
 
 def PetrovGalerkinBF(obs, src, tree_o: Tree, tree_s: Tree, k: float, tol: float = 1e-3,
                      alpha: float = 1.0, c_tau: float = 2.9592, adaptive: bool = True,
                      seed: int = 0, minbflvl: int = 3, leafcomp: bool = True,
                      min_samples: int = 10, rank_mode: int = 0, surrogate=None,
-                     keep_mixed: bool = True, ctx: Context | None = None) -> Operator:
+                     keep_mixed: bool = True, ctx: Context | None = None,
+                     factor_storage: int = BF_STORE_C32) -> Operator:
     """Far-field part of ``PetrovGalerkinBF`` (``farfieldonly=true``) on the GPU."""
     far, _ = nearandfar(tree_o, tree_s, alpha, minbflvl, leafcomp)
     return _build(obs, src, tree_o, tree_s, far, k, tol, c_tau, adaptive, seed, min_samples,
-                  rank_mode, surrogate, keep_mixed, ctx)
+                  rank_mode, surrogate, keep_mixed, ctx, factor_storage)

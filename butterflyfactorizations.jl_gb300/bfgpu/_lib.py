@@ -10,6 +10,7 @@ LIB_PATH = os.path.join(_HERE, "libbfgpu.so")
 BF_OK, BF_EINVAL, BF_ENOMEM, BF_ECUDA, BF_ETIMEOUT, BF_ENOTSUP, BF_ESTATE = range(7)
 BF_OP_N, BF_OP_C, BF_OP_T = 0, 1, 2
 BF_PTR_HOST, BF_PTR_DEVICE = 0, 1
+BF_STORE_C32, BF_STORE_FF = 0, 1
 RANK_REC_LEN = 18  # BF_RANK_REC_LEN
 SUR_NW = 4553      # rank-surrogate weight count (bf_surrogate_nweights)
 
@@ -20,7 +21,8 @@ P = C.POINTER
 class BuildOpts(C.Structure):
     _fields_ = [("c_tau", f64), ("min_samples", i32), ("adaptive", i32), ("seed", u64),
                 ("rank_mode", i32), ("keep_mixed", i32), ("surrogate_weights", P(C.c_float)),
-                ("surrogate_nweights", i64), ("surrogate_margin", f64)]
+                ("surrogate_nweights", i64), ("surrogate_margin", f64),
+                ("factor_storage", i32)]
 
 
 class TrainOpts(C.Structure):
@@ -73,11 +75,16 @@ SIGNATURES = [
     ("bf_surrogate_predict", C.c_int, [vp, P(C.c_float), P(C.c_float), i64, P(C.c_float)]),
     ("bf_build", C.c_int, [vp, P(f64), i64, P(f64), i64, vp, vp, P(i64), P(i64), i64, f64, f64,
                            P(BuildOpts), P(vp)]),
+    ("bf_compress_block", C.c_int, [vp, P(f64), i64, P(f64), i64, P(i64), i32, P(i64), i32, i32,
+                                    u64, f64, f64, P(i32), P(C.c_float), P(i32), P(i32), P(i32),
+                                    P(C.c_float)]),
     ("bf_import_factors", C.c_int, [vp, P(FactorDesc), P(vp)]),
     ("bf_matvec", C.c_int, [vp, C.c_int, i64, vp, i64, vp, i64, P(f64), P(f64), C.c_int, vp]),
     ("bf_matvec_mixed", C.c_int, [vp, C.c_int, i64, vp, i64, vp, i64, P(f64), P(f64), C.c_int,
                                   vp]),
     ("bf_matvec_noalloc", C.c_int, [vp, C.c_int, i64, vp, i64, vp, i64, P(f64), P(f64), vp]),
+    ("bf_op_check", C.c_int, [vp, vp]),
+    ("bf_op_set_wait_limit", C.c_int, [vp, i64]),
     ("bf_op_size", C.c_int, [vp, P(i64), P(i64)]),
     ("bf_op_stats_get", C.c_int, [vp, P(OpStats)]),
     ("bf_op_export_blocks", C.c_int, [vp, i64, i64, P(i64), P(i64), P(i32), P(i32), P(i64),

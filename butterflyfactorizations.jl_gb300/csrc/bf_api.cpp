@@ -109,6 +109,7 @@ void bf_build_opts_default(bf_build_opts* o) {
   o->rank_mode = 0;
   o->keep_mixed = 1;
   o->surrogate_margin = 0.15;
+  o->factor_storage = BF_STORE_C32;
 }
 
 void bf_train_opts_default(bf_train_opts* o) {
@@ -251,6 +252,28 @@ int bf_matvec_mixed(bf_op_t op, int trans, int64_t nrhs, const double* x, int64_
   return run_matvec_mixed(op->op, trans, nrhs, x, ldx, y, ldy, alpha, beta, ptr_mode,
                           (cudaStream_t)stream);
   BF_GUARD_END
+}
+
+int bf_op_check(bf_op_t op, void* stream) {
+  BF_GUARD_BEGIN
+  if (!op) {
+    set_error("bf_op_check: NULL operator");
+    return BF_EINVAL;
+  }
+  Operator& o = op->op;
+  BF_TRY_CUDA(cudaSetDevice(o.ctx->device));
+  BF_TRY_CUDA(cudaStreamSynchronize(stream ? (cudaStream_t)stream : o.stream));
+  return take_device_error(o, "bf_op_check");
+  BF_GUARD_END
+}
+
+int bf_op_set_wait_limit(bf_op_t op, int64_t polls) {
+  if (!op) {
+    set_error("bf_op_set_wait_limit: NULL operator");
+    return BF_EINVAL;
+  }
+  op->op.wait_limit = polls < 0 ? -1 : (long long)polls;
+  return BF_OK;
 }
 
 int bf_op_profile_mixed(bf_op_t op, int trans, int32_t nrep, double* ms, int64_t* bytes,

@@ -405,14 +405,14 @@ size_t qr_smem_bytes(int n, int m, bool with_z) {
 int launch_qr(CTask* d_tasks, int ntasks, float2* d_Z, int32_t* d_permpool, bool smem_z,
               size_t smem, cudaStream_t st) {
   if (ntasks <= 0) return BF_OK;
-  static bool attr_set = false;
-  if (!attr_set) {
-    BF_TRY_CUDA(cudaFuncSetAttribute(qr_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     QR_MAX_SMEM));
-    BF_TRY_CUDA(cudaFuncSetAttribute(qr_kernel<false>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, QR_MAX_SMEM));
-    attr_set = true;
-  }
+  static DeviceOnce attr;
+  BF_TRY(attr.run([] {
+    cudaError_t e = cudaFuncSetAttribute(qr_kernel<true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, QR_MAX_SMEM);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(qr_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                QR_MAX_SMEM);
+  }, "qr_kernel shared memory"));
   if (smem_z)
     qr_kernel<true><<<ntasks, QR_NT, smem, st>>>(d_tasks, d_Z, d_permpool);
   else
@@ -458,12 +458,11 @@ int launch_tsolve(const CTask* d_tasks, int ntasks, const float2* d_Z, const int
                   const int32_t* d_colpool, float2* d_raw, int32_t* d_skel, int max_rank,
                   cudaStream_t st) {
   if (ntasks <= 0) return BF_OK;
-  static bool attr_set = false;
-  if (!attr_set) {
-    BF_TRY_CUDA(cudaFuncSetAttribute(tsolve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     TS_MAX_SMEM_R * TS_MAX_SMEM_R * (int)sizeof(float2)));
-    attr_set = true;
-  }
+  static DeviceOnce attr;
+  BF_TRY(attr.run([] {
+    return cudaFuncSetAttribute(tsolve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                TS_MAX_SMEM_R * TS_MAX_SMEM_R * (int)sizeof(float2));
+  }, "tsolve_kernel shared memory"));
   int rr = max_rank <= TS_MAX_SMEM_R ? max_rank : 0;
   size_t smem = (size_t)rr * rr * sizeof(float2);
   tsolve_kernel<<<ntasks, 128, smem, st>>>(d_tasks, d_Z, d_permpool, d_colpool, d_raw, d_skel,

@@ -1044,13 +1044,16 @@ int build_operator(Context* ctx, const double* obs_xyz, int64_t n_obs, const dou
                    const bf_build_opts& opts, Operator& op) {
   auto t0 = std::chrono::steady_clock::now();
   op.ctx = ctx;
+  op.store_ff = opts.factor_storage == BF_STORE_FF ? 1 : 0;
   {
     Builder b(ctx, to, ts, k, tol, opts, op);
     BF_TRY(b.run(obs_xyz, n_obs, src_xyz, n_src, far_obs, far_src, n_far));
   }
-  // the build's factors are complex FP32 values: packed as such (exact)
+  // the build's factors are complex FP32 values: packed as such (exact), or
+  // widened to float-float entries when the caller asks for 16-byte storage
   auto tp = std::chrono::steady_clock::now();
-  BF_TRY(pack_plan(op.logical, op.plan, op.raw_is_double ? (int)sizeof(float4) : (int)sizeof(float2)));
+  BF_TRY(pack_plan(op.logical, op.plan,
+                   (op.raw_is_double || op.store_ff) ? (int)sizeof(float4) : (int)sizeof(float2)));
   auto tu = std::chrono::steady_clock::now();
   const double compress_s = op.stats.build_compress_seconds;
   const int64_t fallbacks = op.stats.surrogate_fallbacks;

@@ -83,7 +83,7 @@ template <typename FT>
 __global__ void __launch_bounds__(TMA_THREADS) fwd_tma_kernel(
     const int32_t* __restrict__ tlist, int n_tasks, const DTask* __restrict__ tasks,
     const FT* __restrict__ A, const int32_t* __restrict__ maps, float4* __restrict__ ws,
-    int* __restrict__ err) {
+    int* __restrict__ err, long long wait_limit) {
   constexpr int SLOT_E = TmaGeom<FT>::SLOT_E;
   constexpr int NSLOT = TmaGeom<FT>::NSLOT;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(TMA_THREADS) fwd_tma_kernel(
       ch.init(t.M, t.n);
       const int nc = ch.count();
       for (int k = 0; k < nc; ++k) {
-        if (!mbar_wait(empty0 + 8 * slot, ph ^ 1u, err)) {
+        if (!mbar_wait(empty0 + 8 * slot, ph ^ 1u, err, wait_limit)) {
           ok = false;
           break;
         }
@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(TMA_THREADS) fwd_tma_kernel(
 #pragma unroll
     for (int q = 0; q < 4; ++q) acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int k = 0; k < nc; ++k) {
-      bool got = dead ? false : mbar_wait(full0 + 8 * slot, ph, err);
+      bool got = dead ? false : mbar_wait(full0 + 8 * slot, ph, err, wait_limit);
       dead = __any_sync(0xffffffffu, !got);
       int c0, cc, r0, rr;
       ch.get(k, c0, cc, r0, rr);
@@ -269,24 +269,30 @@ __global__ void __launch_bounds__(TMA_THREADS) fwd_tma_kernel(
 template <typename FT>
 static int launch_fwd_tma_t(const int32_t* d_tlist, int n_tasks, const DTask* d_tasks,
                             const FT* d_A, const int32_t* d_maps, float4* d_ws, int* d_err,
-                            int n_sm, cudaStream_t st) {
+                            long long wait_limit, int n_sm, cudaStream_t st) {
   constexpr size_t smem = TmaGeom<FT>::SMEM;
-  BF_TRY_CUDA(cudaFuncSetAttribute(fwd_tma_kernel<FT>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  static DeviceOnce attr;
+  BF_TRY(attr.run([] {
+    return cudaFuncSetAttribute(fwd_tma_kernel<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem);
+  }, "fwd_tma_kernel shared memory"));
+  if (wait_limit < 0) wait_limit = BF_SPIN_LIMIT;
   int grid = std::min(n_tasks, 2 * n_sm);
   fwd_tma_kernel<FT><<<grid, TMA_THREADS, smem, st>>>(d_tlist, n_tasks, d_tasks, d_A, d_maps,
-                                                        d_ws, d_err);
+                                                        d_ws, d_err, wait_limit);
   BF_TRY_CUDA(cudaGetLastError());
   return BF_OK;
 }
 
 int launch_fwd_tma(const int32_t* d_tlist, int n_tasks, const DTask* d_tasks, const float4* d_A,
-                   const float2* d_A2, const int32_t* d_maps, float4* d_ws, int* d_err, int n_sm,
-                   cudaStream_t st) {
+                   const float2* d_A2, const int32_t* d_maps, float4* d_ws, int* d_err,
+                   long long wait_limit, int n_sm, cudaStream_t st) {
   if (n_tasks <= 0) return BF_OK;
   if (d_A2)
-    return launch_fwd_tma_t<float2>(d_tlist, n_tasks, d_tasks, d_A2, d_maps, d_ws, d_err, n_sm, st);
-  return launch_fwd_tma_t<float4>(d_tlist, n_tasks, d_tasks, d_A, d_maps, d_ws, d_err, n_sm, st);
+    return launch_fwd_tma_t<float2>(d_tlist, n_tasks, d_tasks, d_A2, d_maps, d_ws, d_err,
+                                    wait_limit, n_sm, st);
+  return launch_fwd_tma_t<float4>(d_tlist, n_tasks, d_tasks, d_A, d_maps, d_ws, d_err, wait_limit,
+                                  n_sm, st);
 }
 
 }  // namespace bfg

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <chrono>
 #include <cstdint>
 #include <cstdio>
@@ -36,6 +37,34 @@ const char* last_error();
     int s_ = (call);              \
     if (s_ != BF_OK) return s_;   \
   } while (0)
+
+// A CUDA set-up call (a kernel attribute such as its dynamic shared-memory
+// limit) made once per device: cudaFuncSetAttribute applies to the current
+// device only, so a flag per process would leave a second device without it.
+// Safe to race: two threads may both make the (idempotent) call once.
+struct DeviceOnce {
+  std::atomic<uint64_t> done{0};
+  template <typename F>
+  int run(F f, const char* what) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      set_error("%s: cudaGetDevice failed: %s", what, cudaGetErrorString(e));
+      return BF_ECUDA;
+    }
+    const uint64_t bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0;
+    if (bit && (done.load(std::memory_order_acquire) & bit)) return BF_OK;
+    e = f();
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      set_error("%s: %s", what, cudaGetErrorString(e));
+      return BF_ECUDA;
+    }
+    if (bit) done.fetch_or(bit, std::memory_order_release);
+    return BF_OK;
+  }
+};
 
 // Open-addressing hash map from a 128-bit key (two uint64) to V, linear
 // probing, no erase: the host bookkeeping of the builder and the packer
@@ -285,7 +314,14 @@ struct Operator {
   int32_t* d_xperm = nullptr;  // leaf order of the x / y regions (Plan::xperm, yperm)
   int32_t* d_yperm = nullptr;
   int* d_err = nullptr;        // device error word of bounded waits (0 = ok)
-  int fwd_kernel = 0;          // 0 = bulk-copy pipeline where possible, 1 = direct loads
+  // host-visible copy of d_err (pinned, mapped): the last kernel of every
+  // plain matvec moves a non-zero d_err here and clears d_err, so that an
+  // asynchronous call's timeout is seen by the host after the stream has
+  // drained (bf_op_check, or the next call on the handle)
+  int* h_err = nullptr;
+  int* h_err_dev = nullptr;    // device address of h_err
+  long long wait_limit = -1;   // polls of a bounded wait; < 0: the default (about 1 s)
+  int store_ff = 0;            // GPU-built factors widened to float-float (16 B) storage
   // staging of host right-hand sides
   double* d_x = nullptr;
   double* d_y = nullptr;
@@ -315,8 +351,11 @@ int profile_matvec(Operator& op, int trans, int nrep, double* ms, int64_t* bytes
 // The launchers take both factor pointers; the non-null one selects the
 // float-float (d_A) or complex FP32 (d_A2) instantiation.
 int launch_fwd_tma(const int32_t* d_tlist, int n_tasks, const DTask* d_tasks, const float4* d_A,
-                   const float2* d_A2, const int32_t* d_maps, float4* d_ws, int* d_err, int n_sm,
-                   cudaStream_t st);
+                   const float2* d_A2, const int32_t* d_maps, float4* d_ws, int* d_err,
+                   long long wait_limit, int n_sm, cudaStream_t st);
+// Takes (and clears) the host-visible error word of the plain path: BF_OK, or
+// BF_ETIMEOUT with the message set.  Reads host memory only (no CUDA call).
+int take_device_error(Operator& op, const char* what);
 // adjoint (conj) / transpose launches of level s; returns the kernel count or -1
 int launch_adj_stage(const Plan& p, int64_t s, bool conj, const int32_t* d_lists,
                      const DTask* d_tasks, const float4* d_A, const float2* d_A2,

@@ -14,7 +14,6 @@
 #include <algorithm>
 #include <atomic>
 #include <cstdlib>
-#include <string>
 
 #include "bf_dfloat.cuh"
 #include "bf_fwd_warp.cuh"
@@ -24,8 +23,10 @@ namespace bfg {
 namespace {
 
 // raw logical blocks -> packed task matrices: complex FP64 raw data becomes
-// float-float entries (float4), complex FP32 raw data (the GPU build's output)
-// is kept as complex FP32 (float2), which is exact and half the bytes.
+// float-float entries (float4); complex FP32 raw data (the GPU build's output)
+// is kept as complex FP32 (float2), which is exact and half the bytes, or
+// widened to float-float with zero low parts when the build asks for the
+// 16-byte storage.
 template <typename SrcT, typename FT>
 __global__ void repack_kernel(const DSeg* __restrict__ segs, const SrcT* __restrict__ raw,
                               FT* __restrict__ A) {
@@ -67,10 +68,22 @@ __global__ void split_kernel(const double2* __restrict__ x, int64_t n, float4* _
   }
 }
 
-// y = beta*y + alpha*v, v = ws[off + i] (optionally conjugated first)
+// y = beta*y + alpha*v, v = ws[off + i] (optionally conjugated first).
+// The last kernel of a matvec: it also moves a non-zero device error word
+// (a bounded wait of this matvec's level launches gave up) to the host-visible
+// word and clears it, so the next matvec starts clean.
 __global__ void combine_kernel(double2* __restrict__ y, int64_t n, const float4* __restrict__ ws,
                                int64_t off, double2 alpha, double2 beta, int beta_zero,
-                               int conj, const int32_t* __restrict__ perm) {
+                               int conj, const int32_t* __restrict__ perm, int* __restrict__ derr,
+                               int* __restrict__ herr) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const int e = *(volatile int*)derr;
+    if (e != 0) {
+      *(volatile int*)herr = e;
+      *(volatile int*)derr = 0;
+      __threadfence_system();
+    }
+  }
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
        q += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = perm ? perm[q] : q;  // region entry q is point perm[q]
@@ -218,6 +231,7 @@ Operator::~Operator() {
   if (d_ws) cudaFree(d_ws);
   if (d_lists) cudaFree(d_lists);
   if (d_err) cudaFree(d_err);
+  if (h_err) cudaFreeHost(h_err);
   if (d_xperm) cudaFree(d_xperm);
   if (d_yperm) cudaFree(d_yperm);
   if (d_x) cudaFree(d_x);
@@ -230,9 +244,10 @@ int upload_plan(Operator& op) {
   BF_TRY_CUDA(cudaSetDevice(op.ctx->device));
   if (!op.stream) BF_TRY_CUDA(cudaStreamCreateWithFlags(&op.stream, cudaStreamNonBlocking));
   // FP64 factors -> float-float (16 B), complex FP32 factors (GPU build) stay
-  // complex FP32 (8 B); two entries of tail padding serve the 16-byte rounding
-  // of the bulk copies (bf_fwd_tma.cu)
-  const bool f32 = !op.raw_is_double;
+  // complex FP32 (8 B) unless the build asked for float-float storage (the
+  // 16-byte layout of FP64 imports; the low parts are zero); two entries of
+  // tail padding serve the 16-byte rounding of the bulk copies (bf_fwd_tma.cu)
+  const bool f32 = !op.raw_is_double && !op.store_ff;
   const size_t esz = f32 ? sizeof(float2) : sizeof(float4);
   if ((size_t)p.fac_bytes != esz) {
     set_error("upload: plan packed for %d-byte factors, data has %zu", p.fac_bytes, esz);
@@ -259,6 +274,9 @@ int upload_plan(Operator& op) {
     if (op.raw_is_double)
       repack_kernel<double2, float4><<<(unsigned)p.segs.size(), 128, 0, op.stream>>>(
           d_segs, (const double2*)op.d_raw, op.d_A);
+    else if (!f32)
+      repack_kernel<float2, float4><<<(unsigned)p.segs.size(), 128, 0, op.stream>>>(
+          d_segs, (const float2*)op.d_raw, op.d_A);
     else
       repack_kernel<float2, float2><<<(unsigned)p.segs.size(), 128, 0, op.stream>>>(
           d_segs, (const float2*)op.d_raw, op.d_A2);
@@ -286,12 +304,9 @@ int upload_plan(Operator& op) {
   BF_TRY_CUDA(cudaMemset(op.d_ws, 0, (size_t)std::max<int64_t>(p.ws_entries, 1) * sizeof(float4)));
   BF_TRY_CUDA(cudaMalloc(&op.d_err, sizeof(int)));
   BF_TRY_CUDA(cudaMemset(op.d_err, 0, sizeof(int)));
-  {
-    // forward kernel family: the bulk-copy pipeline unless the caller asks for
-    // the direct-load kernels (used to compare the two in benchmarks)
-    const char* fk = getenv("BFGPU_FWD_KERNEL");
-    op.fwd_kernel = (fk && std::string(fk) == "direct") ? 1 : 0;
-  }
+  BF_TRY_CUDA(cudaHostAlloc((void**)&op.h_err, sizeof(int), cudaHostAllocMapped));
+  *(volatile int*)op.h_err = 0;
+  BF_TRY_CUDA(cudaHostGetDevicePointer((void**)&op.h_err_dev, op.h_err, 0));
   BF_TRY_CUDA(cudaMalloc(&op.d_xperm, std::max<size_t>(1, p.xperm.size()) * sizeof(int32_t)));
   BF_TRY_CUDA(cudaMemcpy(op.d_xperm, p.xperm.data(), p.xperm.size() * sizeof(int32_t),
                          cudaMemcpyHostToDevice));
@@ -314,9 +329,11 @@ int upload_plan(Operator& op) {
   return BF_OK;
 }
 
-// Forward launches of level s with factor entries of type FT.
+// Forward launches of level s with factor entries of type FT; adds the
+// number of kernels launched to *nk.
 template <typename FT>
-static int launch_fwd_stage(Operator& op, int64_t s, cudaStream_t st, float4* ws, const FT* A) {
+static int launch_fwd_stage(Operator& op, int64_t s, cudaStream_t st, float4* ws, const FT* A,
+                            int64_t* nk_out) {
   const Plan& p = op.plan;
   int nk = 0;
   auto range = [&](int c, int64_t& b, int64_t& n) {
@@ -327,7 +344,7 @@ static int launch_fwd_stage(Operator& op, int64_t s, cudaStream_t st, float4* ws
   const unsigned WT = FW_WARPS * 32;
   // short wide tasks (the P stage) stream through the bulk-copy pipeline; the
   // many small R-level tasks and the tall Q tasks run the direct-load kernels
-  const bool tma_wide = p.stage_tma[s] && op.fwd_kernel == 0;
+  const bool tma_wide = p.stage_tma[s] != 0;
   range(Plan::L_TALL, b, n);
   if (n > 0) {
     int64_t items = n / 2;
@@ -350,7 +367,7 @@ static int launch_fwd_stage(Operator& op, int64_t s, cudaStream_t st, float4* ws
   range(Plan::L_WIDE, b, n);
   if (n > 0 && tma_wide) {
     BF_TRY(launch_fwd_tma(op.d_lists + b, (int)n, op.d_tasks, op.d_A, op.d_A2, op.d_maps, ws,
-                          op.d_err, op.ctx->prop.multiProcessorCount, st));
+                          op.d_err, op.wait_limit, op.ctx->prop.multiProcessorCount, st));
     ++nk;
   } else if (n > 0) {
     fwd_wide_kernel<FT><<<(unsigned)n, 256, 0, st>>>(op.d_lists + b, op.d_tasks, A, op.d_maps, ws);
@@ -362,27 +379,31 @@ static int launch_fwd_stage(Operator& op, int64_t s, cudaStream_t st, float4* ws
                                                          op.d_maps, ws, 0);
     ++nk;
   }
-  return nk;
+  BF_TRY_CUDA(cudaGetLastError());
+  if (nk_out) *nk_out += nk;
+  return BF_OK;
 }
 
-// Launches of level s for direction trans; returns the number of kernels.
-static int launch_stage(Operator& op, int64_t s, int trans, cudaStream_t st, float4* ws) {
+// Launches of level s for direction trans; adds the kernel count to *nk.
+static int launch_stage(Operator& op, int64_t s, int trans, cudaStream_t st, float4* ws,
+                        int64_t* nk_out) {
   const Plan& p = op.plan;
-  int nk = 0;
   if (trans == BF_OP_N)
-    return op.d_A2 ? launch_fwd_stage<float2>(op, s, st, ws, op.d_A2)
-                   : launch_fwd_stage<float4>(op, s, st, ws, op.d_A);
+    return op.d_A2 ? launch_fwd_stage<float2>(op, s, st, ws, op.d_A2, nk_out)
+                   : launch_fwd_stage<float4>(op, s, st, ws, op.d_A, nk_out);
   // adjoint / transpose: same tasks, rows and columns swapped
-  nk = launch_adj_stage(p, s, trans == BF_OP_C, op.d_lists, op.d_tasks, op.d_A, op.d_A2,
-                        op.d_maps, ws, st);
-  if (nk < 0) return 0;
+  int nk = launch_adj_stage(p, s, trans == BF_OP_C, op.d_lists, op.d_tasks, op.d_A, op.d_A2,
+                            op.d_maps, ws, st);
+  if (nk < 0) return BF_ECUDA;  // message set by the launcher
   int64_t b = p.list_begin[Plan::L_COPY][s], n = p.list_begin[Plan::L_COPY][s + 1] - b;
   if (n > 0) {
     copy_kernel<<<(unsigned)((n + 7) / 8), 256, 0, st>>>(op.d_lists + b, (int)n, op.d_tasks,
                                                          op.d_maps, ws, 1);
     ++nk;
   }
-  return nk;
+  BF_TRY_CUDA(cudaGetLastError());
+  if (nk_out) *nk_out += nk;
+  return BF_OK;
 }
 
 // One FP64-accurate matvec of a single right-hand side, device pointers.
@@ -400,12 +421,22 @@ static int matvec_one(Operator& op, int trans, const double2* x, double2* y, dou
   if (!covered)
     BF_TRY_CUDA(cudaMemsetAsync(ws + out_off, 0, (size_t)nout * sizeof(float4), st));
   const int64_t ns = p.n_stages();
-  for (int64_t k = 0; k < ns; ++k) launch_stage(op, fwd ? k : ns - 1 - k, trans, st, ws);
+  for (int64_t k = 0; k < ns; ++k) BF_TRY(launch_stage(op, fwd ? k : ns - 1 - k, trans, st, ws, nullptr));
   combine_kernel<<<grid_for(nout, 256), 256, 0, st>>>(y, nout, ws, out_off, alpha, beta,
                                                       beta.x == 0.0 && beta.y == 0.0, 0,
-                                                      fwd ? op.d_yperm : op.d_xperm);
+                                                      fwd ? op.d_yperm : op.d_xperm, op.d_err,
+                                                      op.h_err_dev);
   BF_TRY_CUDA(cudaGetLastError());
   return BF_OK;
+}
+
+int take_device_error(Operator& op, const char* what) {
+  if (!op.h_err) return BF_OK;
+  const int e = __atomic_exchange_n(op.h_err, 0, __ATOMIC_ACQ_REL);
+  if (e == 0) return BF_OK;
+  set_error("%s: a bounded device-side wait of a matvec on this operator gave up (code %d); "
+            "that matvec's output is invalid", what, e);
+  return BF_ETIMEOUT;
 }
 
 // Per-stage device time of one matvec: events around every level launch.
@@ -425,7 +456,7 @@ int profile_matvec(Operator& op, int trans, int nrep, double* ms, int64_t* bytes
     BF_TRY_CUDA(cudaEventRecord(ev[0], st));
     int64_t cnt = 2;
     for (int64_t k = 0; k < ns; ++k) {
-      cnt += launch_stage(op, fwd ? k : ns - 1 - k, trans, st, op.d_ws);
+      BF_TRY(launch_stage(op, fwd ? k : ns - 1 - k, trans, st, op.d_ws, &cnt));
       BF_TRY_CUDA(cudaEventRecord(ev[k + 1], st));
     }
     BF_TRY_CUDA(cudaGetLastError());
@@ -445,6 +476,14 @@ int profile_matvec(Operator& op, int trans, int nrep, double* ms, int64_t* bytes
     if (bytes) bytes[s] = p.stage_bytes[s];
   }
   if (kernels) *kernels = nk;
+  // the level launches ran without the combine kernel: read the device word here
+  int h = 0;
+  BF_TRY_CUDA(cudaMemcpy(&h, op.d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h != 0) {
+    BF_TRY_CUDA(cudaMemset(op.d_err, 0, sizeof(int)));
+    set_error("bf_op_profile: a bounded device-side wait gave up (code %d)", h);
+    return BF_ETIMEOUT;
+  }
   return BF_OK;
 }
 
@@ -464,6 +503,8 @@ int run_matvec(Operator& op, int trans, int64_t nrhs, const double* x, int64_t l
     return BF_EINVAL;
   }
   if (nrhs == 0) return BF_OK;
+  // a timeout of an earlier asynchronous call that nobody has collected yet
+  BF_TRY(take_device_error(op, "bf_matvec"));
   double2 a = make_double2(alpha ? alpha[0] : 1.0, alpha ? alpha[1] : 0.0);
   double2 b = make_double2(beta ? beta[0] : 0.0, beta ? beta[1] : 0.0);
   const bool bzero = b.x == 0.0 && b.y == 0.0;
@@ -501,7 +542,7 @@ int run_matvec(Operator& op, int trans, int64_t nrhs, const double* x, int64_t l
   BF_TRY_CUDA(cudaMemcpy2DAsync(y, ldy * 2 * sizeof(double), op.d_y, nout * 2 * sizeof(double),
                                 nout * 2 * sizeof(double), nrhs, cudaMemcpyDeviceToHost, st));
   BF_TRY_CUDA(cudaStreamSynchronize(st));
-  return BF_OK;
+  return take_device_error(op, "bf_matvec");
 }
 
 }  // namespace bfg
@@ -510,13 +551,14 @@ int run_matvec(Operator& op, int trans, int64_t nrhs, const double* x, int64_t l
 // Allocation-free matvec (bf_matvec_noalloc).
 //
 // Some callers must apply the operator at a point where they cannot allocate
-// device memory: a solver step replayed inside a captured CUDA graph, a
-// callback that runs while the caller's memory pool is locked or already
-// exhausted, or a real-time loop whose allocation budget is fixed at start-up.
-// For them the level workspace (the scratch vectors between butterfly levels)
-// lives in one file-scope device array of fixed size instead of the
-// operator's own buffer.  The array is reserved in every GPU's memory as soon
-// as the library is loaded and stays there until the process exits.
+// device memory: a callback that runs while the caller's memory pool is
+// locked or already exhausted (an iterative solver embedded in an application
+// that owns all device memory), or a real-time loop whose allocation budget is
+// fixed at start-up.  For them the level workspace (the scratch vectors
+// between butterfly levels) lives in one file-scope device array of fixed
+// size instead of the operator's own buffer.  The array is reserved in every
+// GPU's memory as soon as the library is loaded and stays there until the
+// process exits.
 namespace bfg {
 namespace {
 
@@ -565,6 +607,7 @@ extern "C" int bf_matvec_noalloc(bf_op_t h, int trans, int64_t nrhs, const doubl
   }
   Operator& op = h->op;
   const Plan& p = op.plan;
+  int s_pre = BF_OK;
   if (trans != BF_OP_N && trans != BF_OP_C && trans != BF_OP_T) {
     set_error("bf_matvec_noalloc: invalid trans %d", trans);
     return BF_EINVAL;
@@ -582,6 +625,9 @@ extern "C" int bf_matvec_noalloc(bf_op_t h, int trans, int64_t nrhs, const doubl
     return BF_EINVAL;
   }
   if (nrhs == 0) return BF_OK;
+  // a timeout of an earlier call on this operator (read from host memory)
+  s_pre = take_device_error(op, "bf_matvec_noalloc");
+  if (s_pre != BF_OK) return s_pre;
   if (cudaSetDevice(op.ctx->device) != cudaSuccess) {
     cudaGetLastError();
     set_error("bf_matvec_noalloc: cudaSetDevice failed");

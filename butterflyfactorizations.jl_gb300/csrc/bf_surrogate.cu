@@ -306,13 +306,11 @@ int grad_pass(const float* d_w, const float* d_f, const float* d_t, const int32_
 }
 
 int set_grad_attr() {
-  static bool done = false;
-  if (!done) {
-    BF_TRY_CUDA(cudaFuncSetAttribute(sur_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)GRAD_SMEM));
-    done = true;
-  }
-  return BF_OK;
+  static DeviceOnce attr;
+  return attr.run([] {
+    return cudaFuncSetAttribute(sur_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)GRAD_SMEM);
+  }, "sur_grad_kernel shared memory");
 }
 
 }  // namespace

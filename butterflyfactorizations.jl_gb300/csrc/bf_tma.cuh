@@ -48,11 +48,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
 }
 
 // Wait until the phase with the given parity of barrier `bar` has completed.
-// Returns false after BF_SPIN_LIMIT polls (setting *err), or as soon as
-// another thread has set *err, so that every waiter leaves promptly once one
-// of them has given up.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err) {
-  for (long long it = 0; it < BF_SPIN_LIMIT; ++it) {
+// Returns false after `limit` polls (setting *err), or as soon as another
+// thread has set *err, so that every waiter leaves promptly once one of them
+// has given up.  The default limit is about a second of polling; the plain
+// path's bulk-copy kernel takes it from the operator, so that a test can make
+// its waits run out (bf_op_set_wait_limit).
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err,
+                                          long long limit = BF_SPIN_LIMIT) {
+  for (long long it = 0; it < limit; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
     if (it > 32) {
       __nanosleep(64);
@@ -64,7 +67,8 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* er
 }
 
 // Bounded wait that ignores *err: used to let the block's own bulk copies
-// land before it exits.
+// land before it exits.  Its limit is always the default one: copies that
+// were issued do complete, and the block must not exit before they have.
 __device__ __forceinline__ bool mbar_wait_drain(uint32_t bar, uint32_t parity, int* err) {
   for (long long it = 0; it < BF_SPIN_LIMIT; ++it) {
     if (mbar_try_wait(bar, parity)) return true;

@@ -126,7 +126,18 @@ typedef struct {
   int64_t surrogate_nweights;
   double surrogate_margin; /* log-rank safety margin of surrogate-seeded sample
                               counts: rows = ceil(exp(pred + margin) / 0.8) + 2 */
+  int32_t factor_storage;  /* BF_STORE_C32 (default): complex FP32 entries, 8 B,
+                              exact for the build's FP32 values; BF_STORE_FF:
+                              float-float entries, 16 B, the FP64-width layout
+                              that ComplexF64 factors (the reference's acctype,
+                              bfassembly.jl:61) import into                     */
 } bf_build_opts;
+
+/* ---- factor storage of GPU-built operators (bf_build_opts.factor_storage) ---- */
+enum {
+  BF_STORE_C32 = 0,
+  BF_STORE_FF = 1
+};
 
 BF_API void bf_build_opts_default(bf_build_opts* opts);
 
@@ -134,6 +145,27 @@ BF_API int bf_build(bf_ctx_t ctx, const double* obs_xyz, int64_t n_obs, const do
                     int64_t n_src, bf_tree_t obs_tree, bf_tree_t src_tree,
                     const int64_t* far_obs, const int64_t* far_src, int64_t n_far, double k,
                     double tol, const bf_build_opts* opts, bf_op_t* out);
+
+/* One compression of the GPU build, for parity tests: one call of the
+ * PartialQR compressor (src/ButterflyFactorization/compressors.jl:81-165,
+ * without the adaptive re-sampling of :134-151) on the device launches
+ * bf_build uses.  Rows: n_rows observer points sampled from obs_index (n_obs
+ * points) by the keyed bijection that stands in for the reference's
+ * randperm (compressors.jl:101), written to rows_out[n_rows] (optional).
+ * Z_out (optional, complex64 n_rows x n_src, column-major): the sampled
+ * kernel block G(obs[rows[i]], src[src_index[j]]).  Then the pivoted QR with
+ * rtol eps (compressors.jl:128-131): *rank_out; perm_out[n_src] the column
+ * pivot order (positions into src_index); skeleton_out[rank] =
+ * src_index[perm[0..rank)] (compressors.jl:162); T_out (complex64, rank x
+ * n_src, column-major, capacity min(n_rows, n_src) * n_src) the
+ * interpolation matrix R11^-1 Q1^H Z (compressors.jl:155-160).  Host
+ * pointers; synchronous. */
+BF_API int bf_compress_block(bf_ctx_t ctx, const double* obs_xyz, int64_t n_obs_pts,
+                             const double* src_xyz, int64_t n_src_pts, const int64_t* obs_index,
+                             int32_t n_obs, const int64_t* src_index, int32_t n_src,
+                             int32_t n_rows, uint64_t key, double k, double eps,
+                             int32_t* rows_out, float* Z_out, int32_t* rank_out,
+                             int32_t* perm_out, int32_t* skeleton_out, float* T_out);
 
 /* ------------------------------------------------------------------------
  * Learned rank surrogate (no reference counterpart; it replaces the fixed
@@ -217,21 +249,38 @@ BF_API int bf_matvec(bf_op_t op, int trans, int64_t nrhs, const double* x, int64
                      double* y, int64_t ldy, const double* alpha, const double* beta,
                      int ptr_mode, void* stream);
 
+/* Errors of asynchronous matvecs (no reference counterpart: a Julia mul!
+ * raises at the call).  A device-pointer bf_matvec or bf_matvec_noalloc
+ * returns before its kernels have run; when one of its bounded device-side
+ * waits gives up (BF_ETIMEOUT, the output is then invalid), the library notes
+ * it in host memory.  bf_op_check synchronises `stream` (NULL: the handle's
+ * own stream) and returns BF_ETIMEOUT if such a timeout happened since the
+ * last check, else BF_OK; the next matvec call on the handle also reports it
+ * (and then does no work).  Host-pointer calls report their own timeout. */
+BF_API int bf_op_check(bf_op_t op, void* stream);
+
+/* Test hook of the timeout path (no reference counterpart): the number of
+ * polls a bounded wait of this operator's plain-path bulk-copy kernel makes
+ * before it gives up.  polls < 0 restores the default (about one second of
+ * polling); 0 makes every such wait give up at once. */
+BF_API int bf_op_set_wait_limit(bf_op_t op, int64_t polls);
+
 /* Allocation-free FP64-accurate matvec on device pointers.  No counterpart in
  * the reference (the Julia package always allocates through its workspaces).
  * For callers that cannot allocate device memory when they apply the
- * operator: a solver step replayed inside a captured CUDA graph, a callback
- * running while the caller's memory pool is locked or exhausted, a real-time
- * loop with a fixed allocation budget.  Same arguments as bf_matvec with
- * ptr_mode = BF_PTR_DEVICE.  The level workspace is one file-scope device
- * array of 16 MiB (1,048,576 complex entries) that every GPU loading the
- * library holds until the process exits; operators whose workspace
+ * operator: a callback running while the caller's memory pool is locked or
+ * exhausted (a solver inside an application that owns all device memory), a
+ * real-time loop with a fixed allocation budget.  Same arguments as bf_matvec
+ * with ptr_mode = BF_PTR_DEVICE.  The level workspace is one file-scope
+ * device array of 16 MiB (1,048,576 complex entries) that every GPU loading
+ * the library holds until the process exits; operators whose workspace
  * (bf_op_stats.workspace_entries) is larger are rejected with BF_EINVAL.
  * The first call on a device looks up the array's device address (and the
  * driver may load kernel code), so make that first call before any stream
  * capture.  All calls share the array and it keeps the last call's
  * contents: calls that overlap on the GPU (for example, issued on two
- * streams) race with each other; serialise them. */
+ * streams) race with each other; serialise them.  The call is asynchronous:
+ * a device-side timeout is reported by bf_op_check or the next call. */
 BF_API int bf_matvec_noalloc(bf_op_t op, int trans, int64_t nrhs, const double* x, int64_t ldx,
                              double* y, int64_t ldy, const double* alpha, const double* beta,
                              void* stream);
