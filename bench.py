@@ -2,22 +2,27 @@
 """Far-field butterfly matvec throughput on GB300.
 
 Default workload (one GPU): the plain FP64 far-field operator of a
-65,536-point Fibonacci sphere at ~100 points per wavelength^2 (k ~ 45.4),
+262,144-point Fibonacci sphere at ~100 points per wavelength^2 (k ~ 90.8),
 octree with <= 32 points per leaf, isFar(alpha=1) admissibility, tol 1e-4,
 one complex Gaussian right-hand side.  Factors are built on the GPU by
-bf_build before timing; a step is one forward far-field matvec over all
-653,570 butterflies.  The factor stream (~5 GB) is far larger than L2, so no
-explicit L2 flush is needed between steps.
+bf_build before timing and stored as float-float entries (16 bytes per complex
+entry, the width of the reference's ComplexF64 factors); a step is one forward
+far-field matvec over all far blocks.  The factor stream (~67 GB) is far
+larger than L2, so no explicit L2 flush is needed between steps.
 
-The same run measures the batched mixed-precision path on the same operator:
-256 right-hand sides (128 plane waves exp(-ik d.x) + 128 complex Gaussians)
-per step through bf_matvec_mixed, its error against the FP64 GPU matvec and
-against FP64 dense far-field rows on a seeded row sample (bfgpu.verify).
-``--workload sphere262k`` is the 262,144-point sphere (k ~ 90.8) with 2,048
-sampled rows.
+The same run measures
+  * the batched mixed-precision path on the same operator: 256 right-hand
+    sides (128 plane waves exp(-ik d.x) + 128 complex Gaussians) per step
+    through bf_matvec_mixed, its error against the FP64 GPU matvec and against
+    FP64 dense far-field rows on 2,048 seeded rows (bfgpu.verify);
+  * the CPU restatement of the reference matvec on a bounded sample of the far
+    blocks, and the GPU matvec on the same sample (parity on identical factors);
+  * the same operator with complex FP32 factor storage (8 bytes per entry, an
+    extra key: half the bytes, exact for the build's FP32 values).
+``--workload sphere65k`` is the 65,536-point sphere (k ~ 45.4, 256 dense rows).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload NAME] [--no-mixed] [--no-cpu]
+                    [--workload NAME] [--storage ff|c32] [--no-mixed] [--no-cpu]
 
 N > 1 runs independent replicas (one per rank, launched by torch.distributed.run);
 the path has no cross-GPU exchange on a single operator.
@@ -25,6 +30,7 @@ the path has no cross-GPU exchange on a single operator.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -61,7 +67,12 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + sorted(BATCH) + sorted(SURROGATE),
-                    default="sphere65k")
+                    default="sphere262k")
+    ap.add_argument("--storage", choices=["ff", "c32"], default="ff",
+                    help="factor storage of the headline operator: float-float (16 B per "
+                         "entry) or complex FP32 (8 B)")
+    ap.add_argument("--no-c32", action="store_true",
+                    help="skip the extra complex-FP32-storage leg")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg")
     ap.add_argument("--mixed-rhs", type=int, default=256)
@@ -318,7 +329,7 @@ def run_ncu_case(args, local):
         b.run()
         print(json.dumps({"ncu_case": args.workload, **b.info()}), flush=True)
         return
-    w = build_workload(args.workload, local)
+    w = build_workload(args.workload, local, args.storage)
     op, n = w["op"], w["n"]
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
@@ -369,7 +380,17 @@ def max_over_ranks(v, world):
     return float(t.item())
 
 
-def build_workload(name, device):
+STORAGE = {"ff": 1, "c32": 0}  # bfgpu.BF_STORE_FF / BF_STORE_C32
+STORAGE_NAME = {"ff": "float-float factors, 16 B per complex entry (the width of ComplexF64)",
+                "c32": "complex FP32 factors, 8 B per complex entry (exact for the build)"}
+
+
+def workload_config(name, w):
+    return (f"{name}: Fibonacci sphere N={w['n']}, k={w['k']:.2f}, octree<=32/leaf, isFar(1.0), "
+            f"tol={w['tol']}, 1 complex Gaussian RHS")
+
+
+def geometry(name):
     import bfgpu
     from bfgpu import geometry as G
     n, leaf, tol = WORKLOADS[name]
@@ -377,13 +398,25 @@ def build_workload(name, device):
     k = G.wavenumber(n, 4.0 * math.pi)
     tree = bfgpu.Tree.build(pts, max_points=leaf)
     far, n_near = bfgpu.nearandfar(tree, tree, 1.0)
-    ctx = bfgpu.Context(device)
-    t0 = time.perf_counter()
-    op = bfgpu.PetrovGalerkinBF(pts, pts, tree, tree, k, tol=tol, ctx=ctx)
-    build_s = time.perf_counter() - t0
     x = G.complex_gaussian(n, 1234)
-    return dict(pts=pts, k=k, tree=tree, far=far, n_near=n_near, ctx=ctx, op=op, x=x, n=n,
-                tol=tol, build_s=build_s)
+    return dict(pts=pts, k=k, tree=tree, far=far, n_near=n_near, x=x, n=n, tol=tol)
+
+
+def build_op(w, ctx, storage):
+    import bfgpu
+    t0 = time.perf_counter()
+    op = bfgpu.PetrovGalerkinBF(w["pts"], w["pts"], w["tree"], w["tree"], w["k"], tol=w["tol"],
+                                ctx=ctx, factor_storage=STORAGE[storage])
+    return op, time.perf_counter() - t0
+
+
+def build_workload(name, device, storage="ff"):
+    import bfgpu
+    w = geometry(name)
+    w["ctx"] = bfgpu.Context(device)
+    w["op"], w["build_s"] = build_op(w, w["ctx"], storage)
+    w["storage"] = storage
+    return w
 
 
 class ClockSampler:
@@ -534,9 +567,7 @@ def run_mixed(args, w, stream, world):
         "roofline": {"bound": "hbm", "achieved": ach_gbs, "peak": hbm, "unit": "GB/s",
                      "frac": ach_gbs / hbm, "peak_source": f"{hbm_kind} hbm_gbs",
                      "traffic": scaled_traffic("mixed", dom, len(sms), sby[dom]),
-                     "traffic_source": "ncu DRAM bytes per level at 16,384 points, scaled by "
-                                       "algorithmic bytes (profiles/dram_traffic_levels_"
-                                       "sphere16k.md)",
+                     "traffic_source": TRAFFIC_SOURCE,
                      "kernel": f"mx_level_kernel, level {dom} of {len(sms)}, one 128-RHS chunk, "
                                f"{sms[dom]:.3f} ms",
                      "tensor_useful_tflops": useful_tf,
@@ -552,14 +583,17 @@ def run_mixed(args, w, stream, world):
     }
 
 
-# DRAM bytes per level launch over the level's algorithmic bytes, by level kind,
-# measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the
-# 16,384-point sphere: profiles/dram_traffic_levels_sphere16k.md.  Traffic
-# grows with the algorithmic bytes (every factor entry and slot is moved once),
-# so a level's traffic at another size is this ratio times its algorithmic
-# bytes.  The R ratio is the one of the largest R level.
-TRAFFIC_RATIO = {"plain": {"Q": 0.976, "R": 0.991, "P": 1.002},
+# DRAM bytes per level launch over the level's algorithmic bytes, by path and
+# level kind, measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum)
+# on the 16,384-point sphere (a capture small enough for a multi-pass ncu
+# run).  Traffic grows with the algorithmic bytes (every factor entry and slot
+# is moved once), so a level's traffic at another size is this ratio times its
+# algorithmic bytes.  The R ratio is the one of the largest R level.
+TRAFFIC_RATIO = {"plain_c32": {"Q": 0.976, "R": 0.991, "P": 1.002},
                  "mixed": {"Q": 0.979, "R": 0.981, "P": 0.999}}
+TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum per level launch at 16,384 "
+                  "points, as a ratio to the level's algorithmic bytes, times this level's "
+                  "algorithmic bytes")
 
 
 def level_kind(dom, n_levels):
@@ -567,31 +601,96 @@ def level_kind(dom, n_levels):
 
 
 def scaled_traffic(path, dom, n_levels, alg_bytes):
-    """DRAM bytes per launch of level dom, scaled from the 16k-point capture."""
-    return int(round(TRAFFIC_RATIO[path][level_kind(dom, n_levels)] * float(alg_bytes)))
+    """DRAM bytes per launch of level dom, scaled from the 16k-point capture (None when
+    that path has no capture)."""
+    r = TRAFFIC_RATIO.get(path)
+    if r is None:
+        return None
+    return int(round(r[level_kind(dom, n_levels)] * float(alg_bytes)))
 
 
-def cpu_baseline(w, reps=3):
-    """Reference flat matvec (oracle C port, OpenMP) on the same factors."""
+# CPU sample: the far blocks [0, bf_end) whose ComplexF64 factors come to about
+# this many bytes (host memory and export time stay bounded at any size)
+CPU_SAMPLE_BYTES = 6 << 30
+CPU_SAMPLE_SECONDS = 10.0
+
+
+def cpu_sample(w, ctx):
+    """A contiguous prefix of the far blocks (depth-first far-pair order) with about
+    CPU_SAMPLE_BYTES of ComplexF64 factors: the exported blocks, the C port of the
+    reference matvec on them, and the same blocks imported back as a GPU operator."""
+    import bfgpu
     from oracle.cbind import CRefOperator
     op = w["op"]
-    ex = op.export_blocks()
+    n_bf = op.stats()["n_bf"]
+    lib = bfgpu.load()
+    nb, nd = ctypes.c_int64(), ctypes.c_int64()
+
+    def data_bytes(end):
+        bfgpu.check(lib.bf_op_export_blocks(op._h, 0, end, ctypes.byref(nb), ctypes.byref(nd),
+                                            *([None] * 11), 0), "export query")
+        return 16 * nd.value
+
+    total = data_bytes(n_bf)
+    lo, hi = 1, n_bf
+    if total > CPU_SAMPLE_BYTES:
+        while lo < hi:  # smallest prefix reaching the byte budget
+            mid = (lo + hi) // 2
+            if data_bytes(mid) >= CPU_SAMPLE_BYTES:
+                hi = mid
+            else:
+                lo = mid + 1
+        end = lo
+    else:
+        end = n_bf
+    ex = op.export_blocks(0, end)
     csr = w["tree"].values_csr()
     cref = CRefOperator(w["n"], w["n"], ex, csr, csr)
+    sub = bfgpu.import_blocks(w["n"], w["n"], ex["bf"], ex["stage"], ex["obs_out"],
+                              ex["src_out"], ex["obs_in"], ex["src_in"], ex["rows"], ex["cols"],
+                              ex["identity"], ex["data_off"], ex["data"], csr, csr, ctx)
+    sample_bytes = data_bytes(end)
     del ex
+    return dict(cref=cref, sub=sub, bf_end=end, n_bf=n_bf, frac=sample_bytes / total,
+                sample_bytes=sample_bytes, total_bytes=total)
+
+
+def time_cpu(cs, x, seconds=CPU_SAMPLE_SECONDS, warmup=1, min_reps=3):
+    """Median time of the C port over the sample, repeated for about `seconds`."""
     threads = os.cpu_count() or 1
-    x = w["x"]
-    y = cref.matvec(x, nthreads=threads)  # warm-up (page-in)
+    y = np.zeros(len(x), np.complex128)
+    for _ in range(max(warmup, 1)):
+        cs["cref"].matvec(x, y, nthreads=threads)
     ts = []
-    for _ in range(reps):
+    t_end = time.perf_counter() + seconds
+    while len(ts) < min_reps or time.perf_counter() < t_end:
         t0 = time.perf_counter()
-        cref.matvec(x, y, nthreads=threads)
+        cs["cref"].matvec(x, y, nthreads=threads)
         ts.append(time.perf_counter() - t0)
-    t = statistics.median(ts)
-    return dict(value=1.0 / t, unit=UNIT, cores=threads, kind="port",
-                sample=f"full far-field matvec ({w['op'].stats()['n_bf']} butterflies, "
-                       f"ComplexF64 factors), median of {reps} after 1 warm-up, "
-                       f"{threads} OpenMP threads"), y
+        if len(ts) >= 1000:
+            break
+    return statistics.median(ts), len(ts), threads, y
+
+
+def sample_text(cs, reps, threads):
+    return (f"far blocks 0..{cs['bf_end'] - 1} of {cs['n_bf']} (a depth-first prefix; "
+            f"{cs['sample_bytes'] / 1e9:.2f} GB of ComplexF64 factors = {100 * cs['frac']:.1f}% "
+            f"of the operator's factor bytes), median of {reps} matvecs, {threads} OpenMP "
+            f"threads; matvecs/s scaled to the whole operator by the factor-byte fraction")
+
+
+def cpu_baseline(w, ctx):
+    """Reference flat matvec (oracle C port, OpenMP) on a bounded sample of the same
+    factors, and parity of the GPU matvec on that sample (imported, identical factors)."""
+    import torch
+    cs = cpu_sample(w, ctx)
+    t, reps, threads, ycpu = time_cpu(cs, w["x"])
+    ygpu = cs["sub"] @ w["x"]
+    torch.cuda.synchronize()
+    parity = float(np.linalg.norm(ygpu - ycpu) / np.linalg.norm(ycpu))
+    cb = dict(value=cs["frac"] / t, unit=UNIT, cores=threads, kind="port",
+              sample=sample_text(cs, reps, threads))
+    return cb, parity, cs["bf_end"]
 
 
 def run_reference(args, rank, world, local):
@@ -602,45 +701,87 @@ def run_reference(args, rank, world, local):
                           "operator batches have no reference counterpart; the batch line's "
                           "cpu_baseline times the reference flat matvec on a sample of it"}))
         return
-    w = build_workload(args.workload, local)
-    from oracle.cbind import CRefOperator
-    ex = w["op"].export_blocks()
-    csr = w["tree"].values_csr()
-    cref = CRefOperator(w["n"], w["n"], ex, csr, csr)
-    del ex
+    import torch
+    torch.cuda.set_device(local)
+    w = build_workload(args.workload, local, args.storage)
+    cs = cpu_sample(w, w["ctx"])
     threads = os.cpu_count() or 1
     x = w["x"]
     y = np.zeros(w["n"], np.complex128)
     for _ in range(args.warmup):
-        cref.matvec(x, y, nthreads=threads)
+        cs["cref"].matvec(x, y, nthreads=threads)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        cref.matvec(x, y, nthreads=threads)
+        cs["cref"].matvec(x, y, nthreads=threads)
     dt = (time.perf_counter() - t0) / args.steps
-    v = 1.0 / dt
+    v = cs["frac"] / dt  # whole-operator matvecs/s
     st = w["op"].stats()
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": f"{args.workload}: Fibonacci sphere N={w['n']}, k={w['k']:.2f}, "
-                               f"octree<=32/leaf, isFar(1.0), tol={w['tol']}, 1 RHS",
-                   "global_batch": 1, "n_far": st["n_bf"], "parallelism": "cpu-openmp"},
+        "config": {"workload": workload_config(args.workload, w), "global_batch": 1,
+                   "n_far": st["n_bf"], "parallelism": "cpu-openmp"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "full far-field matvec per step; factors built by bf_build "
-                                   "and exported as ComplexF64 (the timed code is the C "
-                                   "restatement of bfvector.jl:200-296 + matrixvector.jl:8-65)"},
+                         "sample": "each step: the C restatement of bfvector.jl:200-296 + "
+                                   "matrixvector.jl:8-65 over " +
+                                   sample_text(cs, args.steps, threads) +
+                                   "; factors built by bf_build, exported as ComplexF64"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
+def time_plain(op, xd, yd, n, stream, steps, warmup):
+    """CUDA-event time per forward (or adjoint view) matvec on device pointers."""
+    import torch
+    import bfgpu
+    sp = stream.cuda_stream
+
+    def step():
+        op.matvec_ptr(xd.data_ptr(), n, yd.data_ptr(), n, ptr_mode=bfgpu.BF_PTR_DEVICE, stream=sp)
+
+    for _ in range(max(warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    op.check(sp)
+    return e0.elapsed_time(e1) / steps
+
+
+def plain_roofline(op, storage):
+    """Dominant level launch: algorithmic bytes over its CUDA-event time (inside the
+    library, on the operator's stream), and the whole-matvec rate from the same pass."""
+    stage_ms, stage_bytes, kernels = op.profile(nrep=5)
+    dom = int(np.argmax(stage_ms))
+    achieved = stage_bytes[dom] / (stage_ms[dom] * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak,
+            "traffic": scaled_traffic(f"plain_{storage}", dom, len(stage_ms), stage_bytes[dom]),
+            "traffic_source": TRAFFIC_SOURCE,
+            "kernel": f"level launch {dom} of {len(stage_ms)} "
+                      f"({level_kind(dom, len(stage_ms))} stage), {stage_ms[dom]:.3f} ms",
+            "peak_source": f"{peak_kind} hbm_gbs",
+            "whole_matvec_gbs": float(stage_bytes.sum() / (stage_ms.sum() * 1e-3) / 1e9),
+            "whole_matvec_frac": float(stage_bytes.sum() / (stage_ms.sum() * 1e-3) / 1e9 / peak),
+            "stage_ms": [round(float(v), 4) for v in stage_ms],
+            "stage_bytes": [int(v) for v in stage_bytes]}, kernels
+
+
 def run_ours(args, rank, world, local):
+    import gc
     import torch
     import bfgpu
     torch.cuda.set_device(local)
-    w = build_workload(args.workload, local)
+    w = build_workload(args.workload, local, args.storage)
     op = w["op"]
     n = w["n"]
     st = op.stats()
@@ -675,27 +816,15 @@ def run_ours(args, rank, world, local):
     barrier(world)
     torch.cuda.synchronize()
     clocks = clk.stop()
+    op.check(sp)  # no bounded device wait gave up during the timed steps
     ms = e0.elapsed_time(e1) / args.steps
     ms = max_over_ranks(ms, world)
     value = world * 1000.0 / ms
-
-    # accuracy of this step against sampled dense far-field rows (FP64 sums)
     y = yd.cpu().numpy()
 
     # adjoint throughput (same timing method)
     opa = op.adjoint()
-
-    def astep():
-        opa.matvec_ptr(xd.data_ptr(), n, yd.data_ptr(), n, ptr_mode=bfgpu.BF_PTR_DEVICE, stream=sp)
-
-    for _ in range(3):
-        astep()
-    e0.record(stream)
-    for _ in range(args.steps):
-        astep()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms_adj = e0.elapsed_time(e1) / args.steps
+    ms_adj = time_plain(opa, xd, yd, n, stream, args.steps, 3)
 
     # e2e through the public C ABI with pinned host buffers (copies inside the call)
     xh = torch.from_numpy(w["x"]).pin_memory()
@@ -710,23 +839,19 @@ def run_ours(args, rank, world, local):
 
     # roofline of the dominant level launch (CUDA events inside the library)
     adj_stage_ms, _, _ = opa.profile(nrep=3)
-    stage_ms, stage_bytes, kernels = op.profile(nrep=5)
-    dom = int(np.argmax(stage_ms))
-    achieved = stage_bytes[dom] / (stage_ms[dom] * 1e-3) / 1e9
-    peak, peak_kind = peaks()
-    traffic = scaled_traffic("plain", dom, len(stage_ms), stage_bytes[dom])
+    roof, kernels = plain_roofline(op, w["storage"])
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64 (float-float vectors and sums on FP32 pipes; factors complex FP32 as built)",
+        "dtype": f"f64 (float-float vectors and sums on FP32 pipes; {STORAGE_NAME[w['storage']]})",
         "data": "synthetic",
         "config": {
-            "workload": f"{args.workload}: Fibonacci sphere N={n}, k={w['k']:.2f}, "
-                        f"octree<=32/leaf, isFar(1.0), tol={w['tol']}, 1 complex Gaussian RHS",
+            "workload": workload_config(args.workload, w),
             "global_batch": world, "n_far": st["n_bf"], "parallelism": f"replicas x{world}",
             "l2": "no flush: factor stream per step > L2 (129 MB)",
+            "factor_storage": w["storage"],
             "factor_bytes": st["factor_bytes"], "alg_bytes_per_matvec": st["alg_bytes_fwd"],
             "build_seconds": round(w["build_s"], 3), "compressions": st["compressions"],
             "retries": st["retries"]},
@@ -736,31 +861,51 @@ def run_ours(args, rank, world, local):
                     "hbm_gbs": st["alg_bytes_fwd"] / (ms_adj * 1e-3) / 1e9},
         "e2e": {"value": world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 16 * n,
                 "d2h_bytes_per_step": 16 * n},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic,
-                     "traffic_source": "ncu DRAM bytes per level at 16,384 points, scaled by "
-                                       "algorithmic bytes (profiles/dram_traffic_levels_"
-                                       "sphere16k.md)",
-                     "kernel": f"level launch {dom} of {len(stage_ms)} "
-                               f"({'Q' if dom == 0 else 'P' if dom == len(stage_ms) - 1 else 'R'}"
-                               f" stage), {stage_ms[dom]:.3f} ms",
-                     "peak_source": f"{peak_kind} hbm_gbs",
-                     "stage_ms": [round(float(v), 4) for v in stage_ms],
-                     "stage_bytes": [int(v) for v in stage_bytes]},
+        "roofline": roof,
         "gpu_launches": int(kernels * args.steps),
         "clocks": clocks,
     }
-    if not args.no_mixed:
-        line["mixed"] = run_mixed(args, w, stream, world)
-        line["mixed"]["over_plain"] = line["mixed"]["value"] / value
+    # CPU sample first: its imported GPU copy is freed before the mixed path allocates
     if rank == 0 and not args.no_cpu:
         try:
-            cb, ycpu = cpu_baseline(w)
+            cb, parity, end = cpu_baseline(w, w["ctx"])
             line["cpu_baseline"] = cb
-            line["parity_vs_cpu_port"] = float(np.linalg.norm(y - ycpu) / np.linalg.norm(ycpu))
+            line["parity_vs_cpu_port"] = parity
+            line["parity_sample"] = f"far blocks 0..{end - 1}, imported as ComplexF64"
         except Exception as e:  # report, do not fail the GPU measurement
             line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": 0, "kind": "port",
                                     "sample": f"failed: {e}"}
+        gc.collect()
+    if w["storage"] == "ff" and (not args.no_c32 or not args.no_mixed):
+        # the same operator with complex FP32 factor storage (half the bytes).  It
+        # holds the same factor values (the float-float entries' low parts are
+        # zero), and the mixed path packs its BF16 planes from them: at 262,144
+        # points the 128-RHS mixed workspace alone is ~143 GB, which does not fit
+        # beside the float-float operator, so that one is freed first.
+        del op, opa, w["op"]
+        gc.collect()
+        torch.cuda.synchronize()
+        w["op"], b2 = build_op(w, w["ctx"], "c32")
+        w["storage"] = "c32"
+        op2 = w["op"]
+        ms2 = max_over_ranks(time_plain(op2, xd, yd, n, stream, args.steps, args.warmup), world)
+        y2 = yd.cpu().numpy()
+        ms2a = time_plain(op2.adjoint(), xd, yd, n, stream, args.steps, 3)
+        roof2, _ = plain_roofline(op2, "c32")
+        st2 = op2.stats()
+        line["c32"] = {"value": world * 1000.0 / ms2, "unit": UNIT, "ms_per_step": ms2,
+                       "storage": STORAGE_NAME["c32"], "factor_bytes": st2["factor_bytes"],
+                       "alg_bytes_per_matvec": st2["alg_bytes_fwd"],
+                       "hbm_gbs": st2["alg_bytes_fwd"] / (ms2 * 1e-3) / 1e9,
+                       "adjoint": {"value": world * 1000.0 / ms2a, "ms_per_step": ms2a},
+                       "roofline": roof2, "build_seconds": round(b2, 3),
+                       "rel_diff_vs_ff": float(np.linalg.norm(y2 - y) / np.linalg.norm(y))}
+    if not args.no_mixed:
+        line["mixed"] = run_mixed(args, w, stream, world)
+        line["mixed"]["over_plain"] = line["mixed"]["value"] / value
+        line["mixed"]["factors_from"] = STORAGE_NAME[w["storage"]]
+        if "c32" in line:
+            line["mixed"]["over_plain_c32"] = line["mixed"]["value"] / line["c32"]["value"]
     if rank == 0:
         print(json.dumps(line), flush=True)
 
