@@ -97,6 +97,7 @@ SIGNATURES = [
     ("bf_op_task_shapes", C.c_int, [vp, P(i64), P(i32), P(i32), P(i32), P(i32)]),
     ("bf_op_destroy", C.c_int, [vp]),
     ("bf_batch_create", C.c_int, [vp, P(vp), P(i32), i32, i32, P(vp)]),
+    ("bf_batch_create_op", C.c_int, [vp, P(vp), P(i32), P(i32), i32, i32, P(vp)]),
     ("bf_batch_buffers", C.c_int, [vp, i32, P(vp), P(vp)]),
     ("bf_batch_run", C.c_int, [vp, vp]),
     ("bf_batch_matvec", C.c_int, [vp, P(vp), P(i64), P(vp), P(i64), C.c_int, vp]),

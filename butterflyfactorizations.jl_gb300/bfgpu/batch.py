@@ -9,11 +9,12 @@ from ._lib import BF_PTR_DEVICE, BF_PTR_HOST, check, load
 
 
 class Batch:
-    """Forward FP64-accurate matvecs of several operators in one launch sequence.
+    """FP64-accurate matvecs of several operators in one launch sequence.
 
-    ``ops`` are ``bfgpu.Operator`` objects (same factor storage); ``nrhs[i]``
-    right-hand sides for operator i.  ``matvec(xs)`` takes a list of (n_i,
-    nrhs_i) complex128 arrays and returns the list of products.
+    ``ops`` are ``bfgpu.Operator`` objects or their ``adjoint()`` / ``transpose()``
+    views (same factor storage); ``nrhs[i]`` right-hand sides for operator i.
+    ``matvec(xs)`` takes a list of (n_i, nrhs_i) complex128 arrays and returns
+    the list of products.
     """
 
     def __init__(self, ops, nrhs, ctx, rhs_chunk: int = 8):
@@ -22,10 +23,11 @@ class Batch:
         self.nrhs = [int(r) for r in nrhs]
         self.ctx = ctx
         hs = (C.c_void_p * len(self.ops))(*[o._h.value for o in self.ops])
+        tr = (C.c_int32 * len(self.ops))(*[int(o.trans) for o in self.ops])
         nr = (C.c_int32 * len(self.nrhs))(*self.nrhs)
         h = C.c_void_p()
-        check(lib.bf_batch_create(ctx._h, hs, nr, len(self.ops), int(rhs_chunk), C.byref(h)),
-              "bf_batch_create")
+        check(lib.bf_batch_create_op(ctx._h, hs, tr, nr, len(self.ops), int(rhs_chunk),
+                                     C.byref(h)), "bf_batch_create_op")
         self._h = h
 
     def buffers(self, i: int):
@@ -54,7 +56,7 @@ class Batch:
         ms = C.c_double()
         cfg = (C.c_int32 * 3)()
         check(load().bf_batch_autotune(self._h, int(nrep), C.byref(ms), cfg), "bf_batch_autotune")
-        return ms.value, dict(flat_mmax=cfg[0], bucketed=cfg[1], ctas_per_sm=cfg[2])
+        return ms.value, dict(nr_max=cfg[0], order=cfg[1], ctas_per_sm=cfg[2])
 
     def info(self) -> dict:
         g, w, b = C.c_int64(), C.c_int64(), C.c_int64()

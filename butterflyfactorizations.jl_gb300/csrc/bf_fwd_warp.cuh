@@ -6,7 +6,11 @@
 // routing maps (or a contiguous base), reading every factor entry once with
 // coalesced loads and staging the inputs in warp-private shared memory
 // (xw: FW_XB entries, aw: FLAT_MMAX row accumulators).  They are the level
-// routines of the per-shape kernels (bf_matvec.cu).  Blackwell's paired FP32
+// routines of the per-shape kernels (bf_matvec.cu) and of the operator-batch
+// kernels (bf_batch.cu).  The tall, small and copy routines take NR
+// right-hand sides at once: workspace entry e of right-hand side q is
+// ws[e*S + q] (S >= NR; the single-vector path has NR = S = 1), and every
+// factor entry loaded is applied to all NR of them from registers.  Blackwell's paired FP32
 // instructions (__ffma2_rn and relatives) were measured slower here: a pair
 // costs the FMA pipes as much as two scalar operations, and the operand
 // broadcasts they need add instructions.
@@ -30,30 +34,60 @@ __device__ __forceinline__ float4 ws_in(const DTask& t, const int32_t* __restric
   return t.cbase >= 0 ? ws[t.cbase + j] : ws[cmap[j]];
 }
 
+// workspace entry of column j (input side of a forward task)
+__device__ __forceinline__ long long col_entry(const DTask& t, const int32_t* __restrict__ cmap,
+                                               int j) {
+  return t.cbase >= 0 ? (long long)t.cbase + j : (long long)cmap[j];
+}
+
+// input entries of columns [c0, c0 + nb) for NR right-hand sides (stride S)
+// into xw[j*NR + q]
+template <int NR>
+__device__ __forceinline__ void stage_cols(const DTask& t, const int32_t* __restrict__ cmap,
+                                           const float4* __restrict__ ws, int S, int c0, int nb,
+                                           float4* __restrict__ xw) {
+  const int lane = threadIdx.x & 31;
+  if constexpr (NR == 1) {
+    if (S == 1)  // the single-vector path (S is the literal 1 there)
+      for (int j = lane; j < nb; j += 32) xw[j] = ws_in(t, cmap, ws, c0 + j);
+    else
+      for (int j = lane; j < nb; j += 32) xw[j] = ws[col_entry(t, cmap, c0 + j) * S];
+  } else {
+    for (int e = lane; e < nb * NR; e += 32) {
+      const int j = e / NR, q = e - j * NR;
+      xw[e] = ws[col_entry(t, cmap, c0 + j) * S + q];
+    }
+  }
+}
+
 // In all three routines the first factor batch is issued before the input
 // entries are staged (it does not depend on them), and a partial last batch is
 // loaded at once under predicates, so a warp waits on few serial latencies.
 // (Keeping two batches in flight instead was measured slower: the extra
 // registers cost more occupancy than the overlap gained.)
-template <typename FT>
+template <typename FT, int NR = 1>
 __device__ __forceinline__ void warp_tall(const DTask& t, int r0, const FT* __restrict__ A,
                                           const int32_t* __restrict__ maps,
-                                          float4* __restrict__ ws, float4* __restrict__ xw) {
+                                          float4* __restrict__ ws, float4* __restrict__ xw,
+                                          int S = 1) {
   const int lane = threadIdx.x & 31;
   const int32_t* __restrict__ rmap = maps + t.rmap_off;
   const int32_t* __restrict__ cmap = maps + t.cmap_off;
   const int M = t.M, n = t.n;
   if (r0 >= M) return;
-  float4 acc[TALL_RPL];
+  constexpr int XB = FW_XB / NR;  // staged columns per pass (xw holds XB * NR entries)
+  float4 acc[TALL_RPL][NR];
 #pragma unroll
-  for (int q = 0; q < TALL_RPL; ++q) acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int q = 0; q < TALL_RPL; ++q)
+#pragma unroll
+    for (int v = 0; v < NR; ++v) acc[q][v] = make_float4(0.f, 0.f, 0.f, 0.f);
   bool act[TALL_RPL];
 #pragma unroll
   for (int q = 0; q < TALL_RPL; ++q) act[q] = r0 + lane + 32 * q < M;
   // columns per batch: 128 bytes of factor loads per lane
   constexpr int CPI = (sizeof(FT) == 8 ? 16 : 8) / TALL_RPL;
-  for (int cb = 0; cb < n; cb += FW_XB) {
-    const int nb = min(FW_XB, n - cb);  // warp-uniform
+  for (int cb = 0; cb < n; cb += XB) {
+    const int nb = min(XB, n - cb);  // warp-uniform
     const FT* __restrict__ ap = A + t.a_off + (size_t)cb * M + r0 + lane;
     FT a[CPI][TALL_RPL];
     auto load = [&](FT(&v)[CPI][TALL_RPL], int j) {
@@ -68,13 +102,16 @@ __device__ __forceinline__ void warp_tall(const DTask& t, int r0, const FT* __re
 #pragma unroll
       for (int c = 0; c < CPI; ++c)
         if (j + c < nb) {
-          const float4 xc = xw[j + c];
 #pragma unroll
-          for (int q = 0; q < TALL_RPL; ++q) cdf_mac(acc[q], v[c][q], xc);
+          for (int r = 0; r < NR; ++r) {
+            const float4 xc = xw[(j + c) * NR + r];
+#pragma unroll
+            for (int q = 0; q < TALL_RPL; ++q) cdf_mac(acc[q][r], v[c][q], xc);
+          }
         }
     };
     load(a, 0);
-    for (int j = lane; j < nb; j += 32) xw[j] = ws_in(t, cmap, ws, cb + j);
+    stage_cols<NR>(t, cmap, ws, S, cb, nb, xw);
     __syncwarp();
     for (int j = 0; j < nb; j += CPI) {
       if (j > 0) load(a, j);
@@ -84,7 +121,11 @@ __device__ __forceinline__ void warp_tall(const DTask& t, int r0, const FT* __re
   }
 #pragma unroll
   for (int q = 0; q < TALL_RPL; ++q)
-    if (act[q]) ws[rmap[r0 + lane + 32 * q]] = cdf_norm(acc[q]);
+    if (act[q]) {
+      const long long e = rmap[r0 + lane + 32 * q];
+#pragma unroll
+      for (int r = 0; r < NR; ++r) ws[e * S + r] = cdf_norm(acc[q][r]);
+    }
   __syncwarp();
 }
 
@@ -162,10 +203,11 @@ __device__ __forceinline__ void warp_flat(const DTask& t, const FT* __restrict__
 
 // M <= 32: G = 32/M lane groups walk interleaved columns (one warp load reads
 // G*M contiguous entries); the groups meet in shared memory at the end.
-template <typename FT>
+template <typename FT, int NR = 1>
 __device__ __forceinline__ void warp_small(const DTask& t, const FT* __restrict__ A,
                                            const int32_t* __restrict__ maps,
-                                           float4* __restrict__ ws, float4* __restrict__ xw) {
+                                           float4* __restrict__ ws, float4* __restrict__ xw,
+                                           int S = 1) {
   const int lane = threadIdx.x & 31;
   const int32_t* __restrict__ rmap = maps + t.rmap_off;
   const int32_t* __restrict__ cmap = maps + t.cmap_off;
@@ -173,13 +215,16 @@ __device__ __forceinline__ void warp_small(const DTask& t, const FT* __restrict_
   const int G = 32 / M;
   const int g = lane / M, i = lane - g * M;
   const bool active = g < G;
-  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  constexpr int XB = FW_XB / NR;  // staged columns per pass
+  float4 acc[NR];
+#pragma unroll
+  for (int r = 0; r < NR; ++r) acc[r] = make_float4(0.f, 0.f, 0.f, 0.f);
   // lane group g reads columns g, g+G, g+2G, ...; a batch is LU of them (64
   // bytes per lane)
   constexpr int LU = sizeof(FT) == 8 ? 8 : 4;
   const size_t step = (size_t)G * M;
-  for (int cb = 0; cb < n; cb += FW_XB) {
-    const int nb = min(FW_XB, n - cb);  // warp-uniform
+  for (int cb = 0; cb < n; cb += XB) {
+    const int nb = min(XB, n - cb);  // warp-uniform
     const int nk = (nb + G - 1) / G;   // column steps of group 0 (warp-uniform)
     const FT* __restrict__ ap = A + t.a_off + (size_t)(cb + g) * M + i;
     FT a[LU];
@@ -193,11 +238,14 @@ __device__ __forceinline__ void warp_small(const DTask& t, const FT* __restrict_
 #pragma unroll
       for (int u = 0; u < LU; ++u) {
         const int j = g + (k + u) * G;
-        if (active && j < nb) cdf_mac(acc, v[u], xw[j]);
+        if (active && j < nb) {
+#pragma unroll
+          for (int r = 0; r < NR; ++r) cdf_mac(acc[r], v[u], xw[j * NR + r]);
+        }
       }
     };
     load(a, 0);  // the first factor batch does not wait for the input staging
-    for (int j = lane; j < nb; j += 32) xw[j] = ws_in(t, cmap, ws, cb + j);
+    stage_cols<NR>(t, cmap, ws, S, cb, nb, xw);
     __syncwarp();
     for (int k = 0; k < nk; k += LU) {
       if (k > 0) load(a, k);
@@ -206,29 +254,41 @@ __device__ __forceinline__ void warp_small(const DTask& t, const FT* __restrict_
     __syncwarp();
   }
   if (G > 1) {
-    xw[lane] = acc;  // reuse the staging buffer for the group reduction
+    // reuse the staging buffer for the group reduction (32 * NR <= FW_XB entries)
+#pragma unroll
+    for (int r = 0; r < NR; ++r) xw[lane * NR + r] = acc[r];
     __syncwarp();
     if (active && g == 0) {
-      for (int q = 1; q < G; ++q) cdf_add(acc, xw[q * M + i]);
-      ws[rmap[i]] = cdf_norm(acc);
+      for (int q = 1; q < G; ++q)
+#pragma unroll
+        for (int r = 0; r < NR; ++r) cdf_add(acc[r], xw[(q * M + i) * NR + r]);
+      const long long e = rmap[i];
+#pragma unroll
+      for (int r = 0; r < NR; ++r) ws[e * S + r] = cdf_norm(acc[r]);
     }
   } else if (active) {
-    ws[rmap[i]] = cdf_norm(acc);
+    const long long e = rmap[i];
+#pragma unroll
+    for (int r = 0; r < NR; ++r) ws[e * S + r] = cdf_norm(acc[r]);
   }
   __syncwarp();
 }
 
-// identity blocks: copy the input slot to the output slot (reverse: the other way)
+// identity blocks: copy the input slot to the output slot (reverse: the
+// other way), NR right-hand sides at stride S
+template <int NR = 1>
 __device__ __forceinline__ void warp_copy(const DTask& t, const int32_t* __restrict__ maps,
-                                          float4* __restrict__ ws, int reverse) {
+                                          float4* __restrict__ ws, int reverse, int S = 1) {
   const int lane = threadIdx.x & 31;
   const int32_t* __restrict__ rmap = maps + t.rmap_off;
   const int32_t* __restrict__ cmap = maps + t.cmap_off;
-  for (int i = lane; i < t.M; i += 32) {
+  for (int e = lane; e < t.M * NR; e += 32) {
+    const int i = e / NR, r = e - i * NR;
+    const long long o = (long long)rmap[i] * S + r, c = (long long)cmap[i] * S + r;
     if (reverse)
-      ws[cmap[i]] = ws[rmap[i]];
+      ws[c] = ws[o];
     else
-      ws[rmap[i]] = ws[cmap[i]];
+      ws[o] = ws[c];
   }
 }
 

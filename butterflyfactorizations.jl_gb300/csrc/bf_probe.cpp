@@ -109,9 +109,14 @@ extern "C" int bf_compress_block(bf_ctx_t ctx, const double* obs_xyz, int64_t n_
     if (Z_out)
       BF_TRY_CUDA(cudaMemcpy(Z_out, d_Z, (size_t)n_rows * n_src * sizeof(float2),
                              cudaMemcpyDeviceToHost));
-    // the builder's choice: the block in shared memory when it fits
+    // the builder's choice: the block in shared memory when it fits; either
+    // way the column norms and the permutation (n_src entries) live there
     const bool smem_z = qr_smem_bytes(n_rows, n_src, true) <= (size_t)QR_MAX_SMEM;
-    const size_t smem = smem_z ? qr_smem_bytes(n_rows, n_src, true) : qr_smem_bytes(0, 0, false);
+    const size_t smem = qr_smem_bytes(n_rows, n_src, smem_z);
+    if (smem > (size_t)QR_MAX_SMEM) {
+      set_error("bf_compress_block: %d columns exceed the QR kernel's shared memory", n_src);
+      return BF_EINVAL;
+    }
     BF_TRY(launch_qr(d_task, 1, d_Z, d_perm, smem_z, smem, st));
     BF_TRY_CUDA(cudaMemcpy(&t, d_task, sizeof(CTask), cudaMemcpyDeviceToHost));
     const int r = t.rank;

@@ -376,30 +376,38 @@ BF_API int bf_op_destroy(bf_op_t op);
 
 /* ------------------------------------------------------------------------
  * Batches: many independent operators, each with its own number of right-hand
- * sides, applied by one launch sequence (no reference counterpart: the
- * reference runs each mul! and each column separately, bfmatrix.jl:10-75).
- * Forward, FP64-accurate, y_i = A_i x_i for every operator i and column.  The
- * level sequences are merged (one persistent launch per level for all
- * operators) and captured once as a CUDA graph; right-hand sides run in
- * chunks of rhs_chunk (default 8; one workspace per chunk column).  All
- * operators must have the same factor storage (all GPU-built, or all imported).
- * The operators must outlive the batch. */
+ * sides and its own direction, applied by one launch sequence (no reference
+ * counterpart: the reference runs each mul! and each column separately,
+ * bfmatrix.jl:10-75, and materialises every adjoint, bfadjtr.jl:43-67).
+ * FP64-accurate, y_i = op_i(A_i) x_i for every operator i and column, with
+ * op_i = BF_OP_N, BF_OP_C (adjoint, matrix_adj_tr.jl:8-25) or BF_OP_T
+ * (transpose, matrix_adj_tr.jl:28-40).  The level sequences are merged (one
+ * persistent launch per level and task class for all operators; adjoints walk
+ * their levels backwards) and captured once as a CUDA graph; right-hand sides
+ * run in chunks of rhs_chunk (default 8), and the forward routines apply every
+ * factor entry they load to up to four right-hand sides of a chunk.  All
+ * operators must have the same factor storage (all complex FP32, or all
+ * float-float).  The operators must outlive the batch. */
+BF_API int bf_batch_create_op(bf_ctx_t ctx, bf_op_t const* ops, const int32_t* trans,
+                              const int32_t* nrhs, int32_t n_ops, int32_t rhs_chunk,
+                              bf_batch_t* out);
+/* bf_batch_create_op with every operator forward (trans == NULL). */
 BF_API int bf_batch_create(bf_ctx_t ctx, bf_op_t const* ops, const int32_t* nrhs,
                            int32_t n_ops, int32_t rhs_chunk, bf_batch_t* out);
-/* Device buffers of operator i: x (n_cols x nrhs) and y (n_rows x nrhs),
- * complex double, column-major, leading dimension = size.  bf_batch_run reads
- * every x buffer and writes every y buffer. */
+/* Device buffers of operator i: x (n_in x nrhs) and y (n_out x nrhs), complex
+ * double, column-major, leading dimension = size (n_in = columns of op_i(A_i),
+ * n_out = its rows).  bf_batch_run reads every x buffer and writes every y. */
 BF_API int bf_batch_buffers(bf_batch_t b, int32_t op, double** x_dev, double** y_dev);
 /* one graph launch on stream (NULL: the batch's own stream, synchronised) */
 BF_API int bf_batch_run(bf_batch_t b, void* stream);
-/* copies x[i] (ldx[i] >= n_cols_i; NULL ldx: packed) in, runs, copies y[i] out;
+/* copies x[i] (ldx[i] >= n_in_i; NULL ldx: packed) in, runs, copies y[i] out;
  * ptr_mode BF_PTR_HOST or BF_PTR_DEVICE */
 BF_API int bf_batch_matvec(bf_batch_t b, const double* const* x, const int64_t* ldx,
                            double* const* y, const int64_t* ldy, int ptr_mode, void* stream);
-/* Autotuner: times nrep graph replays for every candidate of (flat/tall task
- * cut at M = 64, 96 or 128; item order longest-first or bucketed by task
- * shape; 2, 4 or 6 persistent CTAs per SM), keeps the fastest.
- * best_cfg[3] = {flat_mmax, bucketed, ctas_per_sm}. */
+/* Autotuner: times nrep graph replays for every candidate of (right-hand sides
+ * per factor load in the forward routines: 1 or 4; item order: longest first
+ * or operator/task order; 2, 4 or 6 persistent CTAs per SM), keeps the
+ * fastest.  best_cfg[3] = {nr_max, order, ctas_per_sm}. */
 BF_API int bf_batch_autotune(bf_batch_t b, int32_t nrep, double* best_ms, int32_t* best_cfg);
 BF_API int bf_batch_info(bf_batch_t b, int64_t* graph_nodes, int64_t* work_items,
                          int64_t* workspace_bytes, int32_t* rhs_chunks);

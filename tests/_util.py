@@ -93,3 +93,26 @@ def export_to_oracle(ex, tree_o, tree_s, k=0.0, tau=0.0):
         ns = d["P"][0].src_out if d["P"] else 0
         out.append(O.BF(d["Q"], R, d["P"], tree_o, tree_s, k, tau, no, ns).wire())
     return out
+
+
+class CsrTree:
+    """The part of the tree contract the oracle matvec uses (``values(node)``),
+    from a node -> values CSR map (ptr, idx)."""
+
+    def __init__(self, ptr, idx):
+        self.ptr = np.asarray(ptr, np.int64)
+        self.idx = np.asarray(idx, np.int64)
+
+    def values(self, node):
+        return self.idx[self.ptr[node]:self.ptr[node + 1]]
+
+
+def oracle_apply(bfs, x, n_out, op="N"):
+    """Oracle far-field product op(A) x over the BF list (reference-order flat
+    matvec of each block, the materialised adjoint / transpose for "C" / "T")."""
+    from oracle import bfref as O
+    y = np.zeros(n_out, np.complex128)
+    for bf in bfs:
+        b = bf if op == "N" else O.adjoint_bf(bf, op)
+        O.matvec_flat(b, x, y, 1.0, 1.0)
+    return y

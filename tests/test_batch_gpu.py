@@ -1,9 +1,15 @@
-"""Batched operators (bf_batch_*): one CUDA-graph launch sequence for several
-operators with different right-hand-side counts must give the same products as
-one bf_matvec per operator (relative 2-norm <= 1e-12 per column: same
-float-float arithmetic, same task routines), for every autotuner candidate.
+"""Batched operators (bf_batch_*) against the oracle.
+
+One CUDA-graph launch sequence applies several operators -- forward, adjoint
+and transpose, each with its own number of right-hand sides -- and every
+column must match the oracle's reference-order product on the same factors
+(oracle.bfref.matvec_flat over the far blocks, with the materialised adjoint of
+src/Butterflyalgebra/bfadjtr.jl:13-67 for op = C / T) to relative 2-norm
+1e-12, for every autotuner candidate.  Operators: the golden fixtures
+(float-float factors imported from the oracle) and small GPU-built operators
+(complex FP32 factors, exported to the oracle exactly).
 """
-import math
+import os
 
 import numpy as np
 import pytest
@@ -11,55 +17,98 @@ import pytest
 import bfgpu
 from bfgpu import geometry as G
 from bfgpu.batch import Batch
+from _util import CsrTree, export_to_oracle, oracle_apply
 
 pytestmark = pytest.mark.gpu
+PARITY = 1e-12
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def golden(name, ctx):
+    g = np.load(os.path.join(HERE, "golden", f"{name}.npz"))
+    op = bfgpu.import_blocks(int(g["n_rows"]), int(g["n_cols"]), g["bf"], g["stage"],
+                             g["obs_out"], g["src_out"], g["obs_in"], g["src_in"], g["rows"],
+                             g["cols"], g["identity"], g["data_off"], g["data"],
+                             (g["obs_ptr"], g["obs_idx"]), (g["src_ptr"], g["src_idx"]), ctx)
+    ex = {k: g[k] for k in ("bf", "stage", "obs_out", "src_out", "obs_in", "src_in", "rows",
+                            "cols", "identity", "data_off", "data")}
+    bfs = export_to_oracle(ex, CsrTree(g["obs_ptr"], g["obs_idx"]),
+                           CsrTree(g["src_ptr"], g["src_idx"]))
+    return op, bfs
+
+
+def view(op, d):
+    return op if d == "N" else op.adjoint() if d == "C" else op.transpose()
+
+
+def check(ops, bfs, dirs, nrhs, ctx, seed, rhs_chunk=8, tune=False):
+    views = [view(o, d) for o, d in zip(ops, dirs)]
+    b = Batch(views, nrhs, ctx, rhs_chunk=rhs_chunk)
+    if tune:
+        ms, cfg = b.autotune(nrep=1)
+        assert ms > 0 and cfg["nr_max"] in (1, 4) and cfg["ctas_per_sm"] in (2, 4, 6)
+    xs = [G.complex_gaussian(v.shape[1], seed + i, nrhs=r)
+          for i, (v, r) in enumerate(zip(views, nrhs))]
+    ys = b.matvec(xs)
+    for v, bf, d, x, y in zip(views, bfs, dirs, xs, ys):
+        for j in range(x.shape[1]):
+            ref = oracle_apply(bf, x[:, j], v.shape[0], d)
+            err = np.linalg.norm(y[:, j] - ref) / np.linalg.norm(ref)
+            assert err <= PARITY, (d, j, err)
+    return b, xs, ys
 
 
 @pytest.fixture(scope="module")
-def ops(ctx):
+def fixtures(ctx):
+    return [golden(n, ctx) for n in ("plane_single", "sphere_far", "plane_unbalanced")]
+
+
+@pytest.fixture(scope="module")
+def built(ctx):
     out = []
-    for shape, n, seed in (("sphere", 4096, 1), ("cube", 3000, 2), ("ellipsoid", 6144, 3)):
+    # small enough for the Python oracle (tens of thousands of far blocks each)
+    for shape, n, seed in (("sphere", 2048, 1), ("cube", 1536, 2), ("ellipsoid", 2560, 3)):
         pts, area = G.shape_points(shape, n, seed)
         k = G.wavenumber(n, area)
         tr = bfgpu.Tree.build(pts, max_points=32)
-        out.append(bfgpu.PetrovGalerkinBF(pts, pts, tr, tr, k, tol=1e-4, ctx=ctx))
+        op = bfgpu.PetrovGalerkinBF(pts, pts, tr, tr, k, tol=1e-4, ctx=ctx)
+        csr = CsrTree(*tr.values_csr())
+        out.append((op, export_to_oracle(op.export_blocks(), csr, csr)))
     return out
 
 
-def colerr(Y, R):
-    return max(np.linalg.norm(Y[:, j] - R[:, j]) / np.linalg.norm(R[:, j])
-               for j in range(R.shape[1]))
+@pytest.mark.parametrize("dirs", [("N", "N", "N"), ("C", "T", "N"), ("T", "N", "C")])
+def test_golden_operators_mixed_directions(fixtures, ctx, dirs):
+    ops = [o for o, _ in fixtures]
+    bfs = [b for _, b in fixtures]
+    # 5 and 11 right-hand sides in chunks of 8: sub-groups of 4, 2 and 1
+    check(ops, bfs, dirs, [1, 5, 11], ctx, seed=10)
 
 
-def test_batch_matches_single_operator_matvecs(ops, ctx):
-    nrhs = [1, 11, 5]
-    b = Batch(ops, nrhs, ctx, rhs_chunk=4)
-    xs = [G.complex_gaussian(o.shape[1], 30 + i, nrhs=r) for i, (o, r) in enumerate(zip(ops, nrhs))]
-    ys = b.matvec(xs)
-    for o, x, y in zip(ops, xs, ys):
-        assert colerr(y, o.matvec(x)) <= 1e-12
+def test_built_operators_and_chunks(built, ctx):
+    ops = [o for o, _ in built]
+    bfs = [b for _, b in built]
+    # 9 right-hand sides in chunks of 4: sub-groups of 4, then a single one
+    b, xs, ys = check(ops, bfs, ("N", "C", "N"), [9, 3, 6], ctx, seed=20, rhs_chunk=4)
     info = b.info()
     assert info["rhs_chunks"] == 3 and info["graph_nodes"] > 0 and info["work_items"] > 0
-    # replay: same result
-    ys2 = b.matvec(xs)
-    for y, y2 in zip(ys, ys2):
+    # replay: same result, bit for bit
+    for y, y2 in zip(ys, b.matvec(xs)):
         assert np.array_equal(y, y2)
 
 
-def test_autotuner_keeps_results(ops, ctx):
-    nrhs = [3, 2, 7]
-    b = Batch(ops, nrhs, ctx, rhs_chunk=8)
-    xs = [G.complex_gaussian(o.shape[1], 40 + i, nrhs=r) for i, (o, r) in enumerate(zip(ops, nrhs))]
-    ms, cfg = b.autotune(nrep=2)
-    assert ms > 0 and cfg["flat_mmax"] in (64, 96, 128) and cfg["ctas_per_sm"] in (2, 4, 6)
-    for o, x, y in zip(ops, xs, b.matvec(xs)):
-        assert colerr(y, o.matvec(x)) <= 1e-12
+def test_autotuner_keeps_results(built, ctx):
+    ops = [o for o, _ in built]
+    bfs = [b for _, b in built]
+    check(ops, bfs, ("T", "N", "C"), [3, 7, 7], ctx, seed=40, tune=True)
 
 
-def test_batch_device_pointers(ops, ctx):
+def test_batch_device_pointers(built, ctx):
     import ctypes as C
     torch = pytest.importorskip("torch")
-    nrhs = [2, 1, 1]
+    ops = [o for o, _ in built]
+    bfs = [b for _, b in built]
+    nrhs = [2, 1, 3]
     b = Batch(ops, nrhs, ctx)
     xs = [G.complex_gaussian(o.shape[1], 50 + i, nrhs=r) for i, (o, r) in enumerate(zip(ops, nrhs))]
     xd = [torch.from_numpy(np.ascontiguousarray(x.T)).cuda() for x in xs]  # column j contiguous
@@ -71,6 +120,20 @@ def test_batch_device_pointers(ops, ctx):
     lib = bfgpu._lib.load()
     assert lib.bf_batch_matvec(b._h, xp, None, yp, None, bfgpu.BF_PTR_DEVICE, None) == 0
     torch.cuda.synchronize()
-    for o, x, y in zip(ops, xs, yd):
-        assert colerr(y.cpu().numpy().T, o.matvec(x)) <= 1e-12
+    for o, bf, x, y in zip(ops, bfs, xs, yd):
+        Y = y.cpu().numpy().T
+        for j in range(x.shape[1]):
+            ref = oracle_apply(bf, x[:, j], o.shape[0])
+            assert np.linalg.norm(Y[:, j] - ref) / np.linalg.norm(ref) <= PARITY
     assert b.buffers(0)[0] != 0
+
+
+def test_batch_matches_single_operator_path(built, ctx):
+    """The same products as one bf_matvec per operator (same arithmetic)."""
+    ops = [o for o, _ in built]
+    views = [view(o, d) for o, d in zip(ops, ("N", "C", "T"))]
+    b = Batch(views, [4, 4, 4], ctx, rhs_chunk=4)
+    xs = [G.complex_gaussian(v.shape[1], 60 + i, nrhs=4) for i, v in enumerate(views)]
+    for v, x, y in zip(views, xs, b.matvec(xs)):
+        ref = v.matvec(x)
+        assert np.linalg.norm(y - ref) / np.linalg.norm(ref) <= PARITY
