@@ -10,6 +10,9 @@ module BFGPU
 
 using LinearAlgebra
 using LinearMaps
+using ButterflyFactorizations: cluster_root, cluster_children, cluster_values, cluster_center,
+                               cluster_radius, cluster_testtree, cluster_trialtree
+import ButterflyFactorizations: PetrovGalerkinBF, assemble_BF
 
 const lib = get(ENV, "BFGPU_LIB", joinpath(@__DIR__, "..", "bfgpu", "libbfgpu.so"))
 
@@ -119,5 +122,186 @@ function import_factors(ctx::Context, bfs, testtree, trialtree, nrows::Integer, 
     end
     return _wrap(h[])
 end
+
+# ---------------------------------------------------------------------------
+# Construction on the GPU.  The reference's calls keep their signatures:
+#   PetrovGalerkinBF(operator, testspace, trialspace, tree, k; tol, ...)
+#       (src/Matrixassembly/petrovgalerkinbf.jl:33-54)
+#   assemble_BF(kernelmatrix, blktree, no, ns, k, tau; ...)
+#       (src/ButterflyFactorization/bfassembly.jl:48-62)
+# with the point Helmholtz kernel G(r) = exp(-ikr)/(4 pi r) as the operator
+# and 3 x N point matrices as the test / trial spaces.  The tree is any tree
+# that implements the reference's tree interface (src/treeinterface.jl:39-164):
+# it is converted once into the library's tree arrays.
+
+"Point Helmholtz kernel exp(-ikr)/(4 pi r): the operator / kernel matrix of the GPU build."
+struct HelmholtzPoints end
+
+# bf_build_opts (include/bfgpu.h), field for field
+struct BuildOpts
+    c_tau::Float64
+    min_samples::Int32
+    adaptive::Int32
+    seed::UInt64
+    rank_mode::Int32
+    keep_mixed::Int32
+    surrogate_weights::Ptr{Float32}
+    surrogate_nweights::Int64
+    surrogate_margin::Float64
+    factor_storage::Int32
+end
+
+const BF_STORE_C32 = Int32(0)
+const BF_STORE_FF = Int32(1)
+
+mutable struct GPUTree
+    h::Ptr{Cvoid}
+    order::Vector{Int}   # library node (0-based position + 1) -> reference node
+end
+
+"""
+    GPUTree(tree, npoints) -> GPUTree
+
+The library's tree arrays (bf_tree_from_arrays) from a tree with the reference
+interface: nodes renumbered breadth first (children contiguous), points in
+depth-first leaf order, so that every node's values are one contiguous range.
+Half-sizes follow the TwoNTree relation radius = halfsize * sqrt(3)
+(ext/BFH2Trees/BFH2Trees.jl:15-16).
+"""
+function GPUTree(tree, npoints::Integer)
+    root = cluster_root(tree)
+    order = [root]
+    first = Int32[]; nchild = Int32[]; parent = Int32[-1]
+    i = 1
+    while i <= length(order)
+        kids = collect(cluster_children(tree, order[i]))
+        push!(first, isempty(kids) ? Int32(0) : Int32(length(order)))
+        push!(nchild, Int32(length(kids)))
+        for c in kids
+            push!(order, c); push!(parent, Int32(i - 1))
+        end
+        i += 1
+    end
+    n = length(order)
+    perm = Int64[]; bgn = zeros(Int64, n); en = zeros(Int64, n)
+    function dfs(k)
+        bgn[k] = length(perm)
+        if nchild[k] == 0
+            append!(perm, cluster_values(tree, order[k]) .- 1)
+        else
+            for c in 0:(nchild[k] - 1)
+                dfs(first[k] + c + 1)
+            end
+        end
+        en[k] = length(perm)
+    end
+    dfs(1)
+    length(perm) == npoints || error("GPUTree: the leaves hold $(length(perm)) of $npoints points")
+    center = Float64[]
+    for nd in order
+        append!(center, collect(cluster_center(tree, nd)))
+    end
+    half = [cluster_radius(tree, nd) / sqrt(3.0) for nd in order]
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:bf_tree_from_arrays, lib), Cint,
+                (Int64, Int64, Ptr{Float64}, Ptr{Float64}, Ptr{Int32}, Ptr{Int32}, Ptr{Int32},
+                 Ptr{Int64}, Ptr{Int64}, Ptr{Int64}, Ref{Ptr{Cvoid}}),
+                n, npoints, center, half, parent, first, nchild, bgn, en, perm, h),
+          "bf_tree_from_arrays")
+    t = GPUTree(h[], order)
+    finalizer(x -> ccall((:bf_tree_destroy, lib), Cint, (Ptr{Cvoid},), x.h), t)
+    return t
+end
+
+"""
+    nearandfar_gpu(testtree, trialtree; alpha, minbflvl, leafcomp, leafimbalance)
+
+Far pairs (library node ids, 0-based) and the near-pair count: the dual-tree
+traversal of src/Matrixassembly/intlists.jl:30-217 with the AABB isFarFunctor
+of ext/BFH2Trees/h2admissible.jl:11-45.
+"""
+function nearandfar_gpu(to::GPUTree, ts::GPUTree; alpha=1.0, minbflvl=3, leafcomp=true,
+                        leafimbalance=true)
+    nf = Ref{Int64}(0); nn = Ref{Int64}(0)
+    args(fo, fs, cap) = ccall((:bf_nearandfar, lib), Cint,
+                              (Ptr{Cvoid}, Ptr{Cvoid}, Float64, Int32, Int32, Int32, Ptr{Int64},
+                               Ptr{Int64}, Int64, Ref{Int64}, Ref{Int64}),
+                              to.h, ts.h, alpha, minbflvl, leafcomp, leafimbalance, fo, fs, cap,
+                              nf, nn)
+    check(args(C_NULL, C_NULL, 0), "bf_nearandfar")
+    fo = zeros(Int64, max(nf[], 1)); fs = zeros(Int64, max(nf[], 1))
+    check(args(fo, fs, length(fo)), "bf_nearandfar")
+    return fo[1:nf[]], fs[1:nf[]], Int(nn[])
+end
+
+function _build(ctx::Context, X::AbstractMatrix{Float64}, Y::AbstractMatrix{Float64},
+                to::GPUTree, ts::GPUTree, fo::Vector{Int64}, fs::Vector{Int64}, k, tol;
+                c_tau, adaptive, seed, min_samples, storage)
+    size(X, 1) == 3 && size(Y, 1) == 3 || error("point sets are 3 x N matrices")
+    o = Ref(BuildOpts(c_tau, min_samples, adaptive, seed, 0, 1, C_NULL, 0, 0.15,
+                      storage === :ff ? BF_STORE_FF : BF_STORE_C32))
+    x = Matrix{Float64}(X); y = Matrix{Float64}(Y)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:bf_build, lib), Cint,
+                (Ptr{Cvoid}, Ptr{Float64}, Int64, Ptr{Float64}, Int64, Ptr{Cvoid}, Ptr{Cvoid},
+                 Ptr{Int64}, Ptr{Int64}, Int64, Float64, Float64, Ref{BuildOpts},
+                 Ref{Ptr{Cvoid}}),
+                ctx.h, x, size(x, 2), y, size(y, 2), to.h, ts.h, fo, fs, length(fo), k, tol, o,
+                h), "bf_build")
+    return _wrap(h[])
+end
+
+"""
+    PetrovGalerkinBF(HelmholtzPoints(), X, Y, tree, k; tol=1e-3, alpha=1.0, Ctau=2.9592,
+                     minbflvl=3, leafcomp=true, leafimbalance=true, adaptive=true,
+                     farfieldonly=true, storage=:c32, ctx=Context(0))
+
+The far field of the reference's PetrovGalerkinBF (petrovgalerkinbf.jl:33-54)
+built on the GPU: the trees of `tree` (cluster_testtree / cluster_trialtree)
+are converted, the far pairs come from nearandfar_gpu, and every far pair is
+compressed by bf_build.  Returns a GPUButterflyOperator (a LinearMap).
+`storage = :ff` keeps the factors as 16-byte float-float entries.
+"""
+function PetrovGalerkinBF(::HelmholtzPoints, X::AbstractMatrix{Float64},
+                          Y::AbstractMatrix{Float64}, tree, k::Float64; tol=1e-3, alpha=1.0,
+                          Ctau=2.9592, minbflvl=3, leafcomp=true, leafimbalance=true,
+                          adaptive=true, farfieldonly=true, seed=0, min_samples=10,
+                          storage=:c32, ctx::Context=Context(0))
+    farfieldonly || error("the GPU operator holds the far field only")
+    to = GPUTree(cluster_testtree(tree), size(X, 2))
+    ts = GPUTree(cluster_trialtree(tree), size(Y, 2))
+    fo, fs, _ = nearandfar_gpu(to, ts; alpha, minbflvl, leafcomp, leafimbalance)
+    return _build(ctx, X, Y, to, ts, fo, fs, k, tol; c_tau=Ctau, adaptive=Int32(adaptive),
+                  seed=UInt64(seed), min_samples=Int32(min_samples), storage)
+end
+
+"""
+    assemble_BF(HelmholtzPoints(), blktree, no, ns, k, tau; X, Y, Ctau=4.0, adaptive=true,
+                storage=:c32, ctx=Context(0))
+
+One far block, as the reference's assemble_BF (bfassembly.jl:48-62): observer
+node `no` of the test tree against source node `ns` of the trial tree (the
+reference's 1-based node ids), compressed on the GPU.
+"""
+function assemble_BF(::HelmholtzPoints, blktree, no::Int, ns::Int, k::Float64, tau::Float64;
+                     X::AbstractMatrix{Float64}, Y::AbstractMatrix{Float64}, Ctau=4.0,
+                     adaptive=true, seed=0, min_samples=10, storage=:c32,
+                     ctx::Context=Context(0))
+    to = GPUTree(cluster_testtree(blktree), size(X, 2))
+    ts = GPUTree(cluster_trialtree(blktree), size(Y, 2))
+    fo = Int64[findfirst(==(no), to.order) - 1]
+    fs = Int64[findfirst(==(ns), ts.order) - 1]
+    return _build(ctx, X, Y, to, ts, fo, fs, k, tau; c_tau=Ctau, adaptive=Int32(adaptive),
+                  seed=UInt64(seed), min_samples=Int32(min_samples), storage)
+end
+
+"""
+    check(A::GPUButterflyOperator)
+
+Raises if a bounded device-side wait of an asynchronous matvec on `A` gave up
+since the last check (bf_op_check).
+"""
+check(A::GPUButterflyOperator) =
+    check(ccall((:bf_op_check, lib), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), A.h, C_NULL), "bf_op_check")
 
 end # module
