@@ -73,6 +73,8 @@ def parse():
                          "entry) or complex FP32 (8 B)")
     ap.add_argument("--no-c32", action="store_true",
                     help="skip the extra complex-FP32-storage leg")
+    ap.add_argument("--no-near", action="store_true",
+                    help="skip the near + far (full operator) leg")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg")
     ap.add_argument("--mixed-rhs", type=int, default=256)
@@ -876,6 +878,26 @@ def run_ours(args, rank, world, local):
             line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": 0, "kind": "port",
                                     "sample": f"failed: {e}"}
         gc.collect()
+    if not args.no_near:
+        # the full PetrovGalerkinBF product: near blocks attached to the same operator,
+        # near + far in one device pass
+        t0 = time.perf_counter()
+        op.add_near(w["pts"], w["pts"], w["tree"], w["tree"], w["k"])
+        near_build_s = time.perf_counter() - t0
+        ms_full = max_over_ranks(time_plain(op, xd, yd, n, stream, args.steps, 3), world)
+        ms_full_adj = time_plain(op.adjoint(), xd, yd, n, stream, args.steps, 3)
+        sn = op.stats()
+        near_ms = max(ms_full - ms, 1e-6)
+        line["near_far"] = {
+            "value": world * 1000.0 / ms_full, "unit": UNIT, "ms_per_step": ms_full,
+            "what": "full PetrovGalerkinBF product: near blocks (FP64-evaluated, float-float, "
+                    "self-term r=0 left out) + far butterflies in one device pass",
+            "adjoint": {"value": world * 1000.0 / ms_full_adj, "ms_per_step": ms_full_adj},
+            "near_pairs": sn["near_pairs"], "near_entries_both_directions": sn["near_entries"],
+            "near_bytes_per_matvec": sn["near_bytes_fwd"],
+            "near_ms_per_matvec": near_ms,
+            "near_hbm_gbs": sn["near_bytes_fwd"] / (near_ms * 1e-3) / 1e9,
+            "near_setup_seconds": round(near_build_s, 3)}
     if w["storage"] == "ff" and (not args.no_c32 or not args.no_mixed):
         # the same operator with complex FP32 factor storage (half the bytes).  It
         # holds the same factor values (the float-float entries' low parts are

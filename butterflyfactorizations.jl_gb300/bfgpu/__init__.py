@@ -24,6 +24,7 @@ All compute runs in ``libbfgpu.so`` on the GPU; there is no CPU fallback.
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -33,7 +34,8 @@ from ._lib import (BF_OP_C, BF_OP_N, BF_OP_T, BF_PTR_DEVICE, BF_PTR_HOST, BF_STO
                    check, load)
 
 __all__ = ["Tree", "Context", "Operator", "nearandfar", "assemble_BF", "PetrovGalerkinBF",
-           "import_blocks", "mul", "BFError", "load"]
+           "import_blocks", "load_operator", "compress_block", "near_pairs", "mul", "BFError",
+           "load"]
 
 
 def _p(a, ct):
@@ -119,6 +121,20 @@ def nearandfar(tree_o: Tree, tree_s: Tree, alpha: float = 1.0, minbflvl: int = 3
     check(lib.bf_nearandfar(*args, _p(fo, C.c_int64), _p(fs, C.c_int64), max(nf.value, 1),
                             C.byref(nf), C.byref(nn)), "bf_nearandfar")
     return np.stack([fo[:nf.value], fs[:nf.value]], axis=1), nn.value
+
+
+def near_pairs(tree_o: Tree, tree_s: Tree, alpha: float = 1.0, minbflvl: int = 3,
+               leafcomp: bool = True, leafimbalance: bool = True):
+    """Near pairs (n_near, 2) [observer node, source node] of the same traversal."""
+    lib = load()
+    nn = C.c_int64()
+    args = (tree_o._h, tree_s._h, float(alpha), int(minbflvl), int(leafcomp), int(leafimbalance))
+    check(lib.bf_near_pairs(*args, None, None, 0, C.byref(nn)), "bf_near_pairs")
+    fo = np.zeros(max(nn.value, 1), np.int64)
+    fs = np.zeros(max(nn.value, 1), np.int64)
+    check(lib.bf_near_pairs(*args, _p(fo, C.c_int64), _p(fs, C.c_int64), max(nn.value, 1),
+                            C.byref(nn)), "bf_near_pairs")
+    return np.stack([fo[:nn.value], fs[:nn.value]], axis=1)
 
 
 class Context:
@@ -329,6 +345,28 @@ class Operator:
               "bf_op_mixed_info")
         return dict(factor_bytes=f.value, workspace_bytes=w.value, work_units=u.value)
 
+    def add_near(self, obs, src, tree_o: Tree, tree_s: Tree, k: float, pairs=None,
+                 alpha: float = 1.0, minbflvl: int = 3, leafcomp: bool = True,
+                 leafimbalance: bool = True):
+        """Attach the near field (``bf_op_add_near``): afterwards every matvec applies
+        near + far, as the reference's ``mul!`` on a full ``PetrovGalerkinBF``."""
+        if pairs is None:
+            pairs = near_pairs(tree_o, tree_s, alpha, minbflvl, leafcomp, leafimbalance)
+        obs = np.ascontiguousarray(obs, np.float64)
+        src = np.ascontiguousarray(src, np.float64)
+        pairs = np.asarray(pairs, np.int64).reshape(-1, 2)
+        no = np.ascontiguousarray(pairs[:, 0])
+        ns = np.ascontiguousarray(pairs[:, 1])
+        check(load().bf_op_add_near(self._h, _p(obs, C.c_double), obs.shape[0],
+                                    _p(src, C.c_double), src.shape[0], tree_o._h, tree_s._h,
+                                    _p(no, C.c_int64), _p(ns, C.c_int64), len(no), float(k)),
+              "bf_op_add_near")
+        return self
+
+    def save(self, path: str):
+        """Write the operator to ``path`` (``bf_op_save``): packed layout and factors."""
+        check(load().bf_op_save(self._h, os.fsencode(path)), "bf_op_save")
+
     def close(self):
         if self._parent is None and self._h and self._h.value:
             load().bf_op_destroy(self._h)
@@ -339,6 +377,14 @@ class Operator:
             self.close()
         except Exception:
             pass
+
+
+def load_operator(path: str, ctx: Context | None = None) -> Operator:
+    """Read an operator written by ``Operator.save`` onto ``ctx``'s device (``bf_op_load``)."""
+    ctx = ctx or default_context()
+    h = C.c_void_p()
+    check(load().bf_op_load(ctx._h, os.fsencode(path), C.byref(h)), "bf_op_load")
+    return Operator(h.value, ctx)
 
 
 def mul(y, A: Operator, x, alpha=1.0, beta=0.0):
@@ -465,8 +511,15 @@ def PetrovGalerkinBF(obs, src, tree_o: Tree, tree_s: Tree, k: float, tol: float 
                      seed: int = 0, minbflvl: int = 3, leafcomp: bool = True,
                      min_samples: int = 10, rank_mode: int = 0, surrogate=None,
                      keep_mixed: bool = True, ctx: Context | None = None,
-                     factor_storage: int = BF_STORE_C32) -> Operator:
-    """Far-field part of ``PetrovGalerkinBF`` (``farfieldonly=true``) on the GPU."""
-    far, _ = nearandfar(tree_o, tree_s, alpha, minbflvl, leafcomp)
-    return _build(obs, src, tree_o, tree_s, far, k, tol, c_tau, adaptive, seed, min_samples,
-                  rank_mode, surrogate, keep_mixed, ctx, factor_storage)
+                     factor_storage: int = BF_STORE_C32,
+                     farfieldonly: bool = True, leafimbalance: bool = True) -> Operator:
+    """``PetrovGalerkinBF`` on the GPU: the far field (``farfieldonly=True``, the default
+    here) or near + far (``farfieldonly=False``, the reference's default; the near blocks
+    leave out the singular self-term r = 0)."""
+    far, _ = nearandfar(tree_o, tree_s, alpha, minbflvl, leafcomp, leafimbalance)
+    op = _build(obs, src, tree_o, tree_s, far, k, tol, c_tau, adaptive, seed, min_samples,
+                rank_mode, surrogate, keep_mixed, ctx, factor_storage)
+    if not farfieldonly:
+        op.add_near(obs, src, tree_o, tree_s, k, alpha=alpha, minbflvl=minbflvl,
+                    leafcomp=leafcomp, leafimbalance=leafimbalance)
+    return op

@@ -45,7 +45,8 @@ class OpStats(C.Structure):
                 ("alg_bytes_fwd", i64), ("max_rank", i64), ("build_seconds", f64),
                 ("compressions", i64), ("retries", i64), ("kernel_entries", i64),
                 ("build_compress_seconds", f64), ("build_pack_seconds", f64),
-                ("build_upload_seconds", f64), ("surrogate_fallbacks", i64)]
+                ("build_upload_seconds", f64), ("surrogate_fallbacks", i64),
+                ("near_pairs", i64), ("near_entries", i64), ("near_bytes_fwd", i64)]
 
 
 # (name, restype, argtypes): every function declared in include/bfgpu.h
@@ -64,6 +65,7 @@ SIGNATURES = [
     ("bf_tree_destroy", C.c_int, [vp]),
     ("bf_nearandfar", C.c_int, [vp, vp, f64, i32, i32, i32, P(i64), P(i64), i64, P(i64),
                                 P(i64)]),
+    ("bf_near_pairs", C.c_int, [vp, vp, f64, i32, i32, i32, P(i64), P(i64), i64, P(i64)]),
     ("bf_build_opts_default", None, [P(BuildOpts)]),
     ("bf_train_opts_default", None, [P(TrainOpts)]),
     ("bf_surrogate_nweights", C.c_int, []),
@@ -78,6 +80,8 @@ SIGNATURES = [
     ("bf_compress_block", C.c_int, [vp, P(f64), i64, P(f64), i64, P(i64), i32, P(i64), i32, i32,
                                     u64, f64, f64, P(i32), P(C.c_float), P(i32), P(i32), P(i32),
                                     P(C.c_float)]),
+    ("bf_op_add_near", C.c_int, [vp, P(f64), i64, P(f64), i64, vp, vp, P(i64), P(i64), i64,
+                                 f64]),
     ("bf_import_factors", C.c_int, [vp, P(FactorDesc), P(vp)]),
     ("bf_matvec", C.c_int, [vp, C.c_int, i64, vp, i64, vp, i64, P(f64), P(f64), C.c_int, vp]),
     ("bf_matvec_mixed", C.c_int, [vp, C.c_int, i64, vp, i64, vp, i64, P(f64), P(f64), C.c_int,
@@ -95,6 +99,8 @@ SIGNATURES = [
     ("bf_op_profile_mixed", C.c_int, [vp, C.c_int, i32, P(f64), P(i64), P(f64), P(i64)]),
     ("bf_op_mixed_info", C.c_int, [vp, P(i64), P(i64), P(i64)]),
     ("bf_op_task_shapes", C.c_int, [vp, P(i64), P(i32), P(i32), P(i32), P(i32)]),
+    ("bf_op_save", C.c_int, [vp, C.c_char_p]),
+    ("bf_op_load", C.c_int, [vp, C.c_char_p, P(vp)]),
     ("bf_op_destroy", C.c_int, [vp]),
     ("bf_batch_create", C.c_int, [vp, P(vp), P(i32), i32, i32, P(vp)]),
     ("bf_batch_create_op", C.c_int, [vp, P(vp), P(i32), P(i32), i32, i32, P(vp)]),

@@ -382,6 +382,11 @@ int bf_batch_create_op(bf_ctx_t ctx, bf_op_t const* ops, const int32_t* trans,
         return BF_EINVAL;
       }
       Operator& op = ops[i]->op;
+      if (op.near) {
+        set_error("bf_batch_create: operator %d has a near field; batches apply far fields "
+                  "(use bf_matvec for near + far)", i);
+        return BF_ENOTSUP;
+      }
       const bool f32 = op.d_A2 != nullptr;
       if (i == 0) b.f32 = f32;
       if (f32 != b.f32) {

@@ -158,6 +158,12 @@ int tree_build(const double* xyz, int64_t n, int32_t max_points, int32_t max_dep
 // BFS levels below root with shallow leaves pushed down (src/auxillaries.jl:263-350).
 std::vector<std::vector<int64_t>> traverse_and_pad(const Tree& t, int64_t root);
 bool is_far(const Tree& ts, const Tree& to, int64_t snode, int64_t onode, double alpha);
+// far and near pairs of the dual-tree traversal (src/Matrixassembly/intlists.jl:30-217)
+void near_far_lists(const Tree& to, const Tree& ts, double alpha, int32_t minbflvl,
+                    int32_t leafcomp, int32_t leafimbalance,
+                    std::vector<std::pair<int64_t, int64_t>>* far,
+                    std::vector<std::pair<int64_t, int64_t>>* near, int64_t* n_far,
+                    int64_t* n_near);
 
 // ---------------------------------------------------------------- logical factors
 // One reference ButterflyBlock (bfstructs.jl:21-29) whose matrix lives in a raw
@@ -288,6 +294,43 @@ struct Plan {
 
 int pack_plan(const Logical& lg, Plan& plan, int fac_bytes);
 
+// ---------------------------------------------------------------- near field
+// The near-field block-sparse part of PetrovGalerkinBF (assembled at
+// src/Matrixassembly/petrovgalerkinbf.jl:57-119, applied at
+// src/matrixalgebra/matrixvector.jl:28-33), as dense tasks in the layout of
+// the far-field levels: tasks [0, n_fwd) are one per observer leaf (rows: its
+// points, written to the near-y workspace region; columns: the points of every
+// source node near the leaf or one of its ancestors, read from the x region);
+// tasks [n_fwd, end) are one per source leaf with the transposed blocks (rows
+// written to the near-x region, columns read from the y region), so each
+// direction has exactly one writer per output entry.
+struct NearField {
+  std::vector<DTask> tasks;
+  int64_t n_fwd = 0;
+  std::vector<int32_t> maps;  // routing entries (workspace entries)
+  // launch lists: small tasks (M <= 32) and tall row panels ((task, row0)
+  // pairs), forward then adjoint; list_begin[c] .. list_begin[c + 1]
+  enum { N_SMALL_F = 0, N_TALL_F, N_SMALL_A, N_TALL_A, N_NCLASS };
+  std::vector<int32_t> lists;
+  int64_t list_begin[N_NCLASS + 1] = {};
+  int64_t a_entries = 0;      // float-float entries, both directions
+  int64_t ny_off = 0, nx_off = 0;
+  int32_t fwd_covered = 0, adj_covered = 0;
+  int64_t n_pairs = 0;
+  int64_t alg_bytes_fwd = 0;  // bytes of one forward near product
+  float4* d_A = nullptr;
+  DTask* d_tasks = nullptr;
+  int32_t* d_maps = nullptr;
+  int32_t* d_lists = nullptr;
+};
+void near_free(NearField* nf);
+int near_upload(NearField& nf);  // tasks, maps, lists (the entries are uploaded by their producer)
+// near-field launches of one matvec into ws (after the far levels, before the combine)
+int near_stage(const struct Operator& op, int trans, cudaStream_t st, float4* ws, int64_t* nk);
+// y_c += alpha * near(op) x_c for nrhs columns (device pointers), through op's workspace
+int near_apply_columns(struct Operator& op, int trans, int64_t nrhs, const double2* x,
+                       int64_t lx, double2* y, int64_t ly, double2 alpha, cudaStream_t st);
+
 // ---------------------------------------------------------------- device-side
 struct Context {
   int device = 0;
@@ -328,6 +371,8 @@ struct Operator {
   int64_t stage_cap = 0;
   // mixed path
   void* mixed = nullptr;
+  // near field (bf_op_add_near), or none
+  NearField* near = nullptr;
   bf_op_stats stats{};
   // per-compression rank records of the build (surrogate training data)
   struct RankRec {
@@ -342,6 +387,7 @@ struct Operator {
 };
 
 int upload_plan(Operator& op);  // repacks d_raw into d_A, uploads tasks/maps, allocates ws
+int upload_tables(Operator& op);  // the plan without the factors (tasks, maps, lists, ws, ...)
 int build_operator(Context* ctx, const double* obs_xyz, int64_t n_obs, const double* src_xyz,
                    int64_t n_src, const Tree& to, const Tree& ts, const int64_t* far_obs,
                    const int64_t* far_src, int64_t n_far, double k, double tol,

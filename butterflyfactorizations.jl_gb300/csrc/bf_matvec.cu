@@ -73,9 +73,9 @@ __global__ void split_kernel(const double2* __restrict__ x, int64_t n, float4* _
 // (a bounded wait of this matvec's level launches gave up) to the host-visible
 // word and clears it, so the next matvec starts clean.
 __global__ void combine_kernel(double2* __restrict__ y, int64_t n, const float4* __restrict__ ws,
-                               int64_t off, double2 alpha, double2 beta, int beta_zero,
-                               int conj, const int32_t* __restrict__ perm, int* __restrict__ derr,
-                               int* __restrict__ herr) {
+                               int64_t off, int64_t off2, double2 alpha, double2 beta,
+                               int beta_zero, int conj, const int32_t* __restrict__ perm,
+                               int* __restrict__ derr, int* __restrict__ herr) {
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     const int e = *(volatile int*)derr;
     if (e != 0) {
@@ -90,6 +90,11 @@ __global__ void combine_kernel(double2* __restrict__ y, int64_t n, const float4*
     float4 a = ws[off + q];
     double vr = (double)a.x + (double)a.y;
     double vi = (double)a.z + (double)a.w;
+    if (off2 >= 0) {  // the near field's region (same leaf order)
+      const float4 b = ws[off2 + q];
+      vr += (double)b.x + (double)b.y;
+      vi += (double)b.z + (double)b.w;
+    }
     if (conj) vi = -vi;
     double2 o;
     o.x = alpha.x * vr - alpha.y * vi;
@@ -223,6 +228,7 @@ inline int grid_for(int64_t n, int threads) {
 
 Operator::~Operator() {
   if (mixed) mixed_free(mixed);
+  if (near) near_free(near);
   if (d_raw) cudaFree(d_raw);
   if (d_A) cudaFree(d_A);
   if (d_A2) cudaFree(d_A2);
@@ -289,6 +295,15 @@ int upload_plan(Operator& op) {
     cudaFree(op.d_raw);
     op.d_raw = nullptr;
   }
+  return upload_tables(op);
+}
+
+// Everything of the plan but the factors: task descriptors, routing maps,
+// launch lists, leaf orders, the level workspace and the error words.
+int upload_tables(Operator& op) {
+  const Plan& p = op.plan;
+  BF_TRY_CUDA(cudaSetDevice(op.ctx->device));
+  if (!op.stream) BF_TRY_CUDA(cudaStreamCreateWithFlags(&op.stream, cudaStreamNonBlocking));
   BF_TRY_CUDA(cudaMalloc(&op.d_tasks, std::max<size_t>(1, p.tasks.size()) * sizeof(DTask)));
   BF_TRY_CUDA(cudaMemcpy(op.d_tasks, p.tasks.data(), p.tasks.size() * sizeof(DTask),
                          cudaMemcpyHostToDevice));
@@ -321,7 +336,7 @@ int upload_plan(Operator& op) {
   op.stats.n_stages = p.n_stages();
   op.stats.n_tasks = (int64_t)p.tasks.size();
   op.stats.factor_entries = p.a_entries;
-  op.stats.factor_bytes = p.a_entries * (int64_t)esz;
+  op.stats.factor_bytes = p.a_entries * (int64_t)p.fac_bytes;
   op.stats.workspace_entries = p.ws_entries;
   op.stats.map_entries = (int64_t)p.maps.size();
   op.stats.alg_bytes_fwd = p.alg_bytes_fwd;
@@ -422,7 +437,12 @@ static int matvec_one(Operator& op, int trans, const double2* x, double2* y, dou
     BF_TRY_CUDA(cudaMemsetAsync(ws + out_off, 0, (size_t)nout * sizeof(float4), st));
   const int64_t ns = p.n_stages();
   for (int64_t k = 0; k < ns; ++k) BF_TRY(launch_stage(op, fwd ? k : ns - 1 - k, trans, st, ws, nullptr));
-  combine_kernel<<<grid_for(nout, 256), 256, 0, st>>>(y, nout, ws, out_off, alpha, beta,
+  int64_t near_off = -1;
+  if (op.near) {  // near + far in one pass (matrixvector.jl:28-33)
+    BF_TRY(near_stage(op, trans, st, ws, nullptr));
+    near_off = fwd ? op.near->ny_off : op.near->nx_off;
+  }
+  combine_kernel<<<grid_for(nout, 256), 256, 0, st>>>(y, nout, ws, out_off, near_off, alpha, beta,
                                                       beta.x == 0.0 && beta.y == 0.0, 0,
                                                       fwd ? op.d_yperm : op.d_xperm, op.d_err,
                                                       op.h_err_dev);

@@ -744,6 +744,8 @@ int run_matvec_mixed(Operator& op, int trans, int64_t nrhs, const double* x, int
     BF_TRY(mixed_chunk(op, trans, nr, xd + c0 * lx, lx, yd + c0 * ly, ly, a, b, st, nullptr,
                        nullptr));
   }
+  // the near field, FP64-accurate, column by column on top of the far field
+  if (op.near) BF_TRY(near_apply_columns(op, trans, nrhs, xd, lx, yd, ly, a, st));
   if (ptr_mode == BF_PTR_HOST)
     BF_TRY_CUDA(cudaMemcpy2DAsync(y, ldy * 2 * sizeof(double), ms.d_y, nout * 2 * sizeof(double),
                                   nout * 2 * sizeof(double), nrhs, cudaMemcpyDeviceToHost, st));

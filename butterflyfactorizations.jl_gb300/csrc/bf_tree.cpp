@@ -250,17 +250,19 @@ int bf_tree_destroy(bf_tree_t tree) {
   return BF_OK;
 }
 
-int bf_nearandfar(bf_tree_t obs_tree, bf_tree_t src_tree, double alpha, int32_t minbflvl,
-                  int32_t leafcomp, int32_t leafimbalance, int64_t* far_obs, int64_t* far_src,
-                  int64_t capacity, int64_t* n_far, int64_t* n_near) {
-  // src/Matrixassembly/intlists.jl:30-217, balanced splitting, explicit stack in
-  // the recursion's depth-first order.
-  if (!obs_tree || !src_tree) {
-    set_error("bf_nearandfar: NULL tree");
-    return BF_EINVAL;
-  }
-  const Tree& to = obs_tree->t;
-  const Tree& ts = src_tree->t;
+}  // extern "C"
+
+namespace bfg {
+
+// Dual-tree traversal of src/Matrixassembly/intlists.jl:30-217 (balanced
+// splitting), an explicit stack in the recursion's depth-first order.  Far
+// pairs go to `far` (when given), near pairs to `near` (when given); both
+// are always counted.
+void near_far_lists(const Tree& to, const Tree& ts, double alpha, int32_t minbflvl,
+                    int32_t leafcomp, int32_t leafimbalance,
+                    std::vector<std::pair<int64_t, int64_t>>* far,
+                    std::vector<std::pair<int64_t, int64_t>>* near, int64_t* n_far,
+                    int64_t* n_near) {
   struct Item {
     int64_t o, s;
     int32_t h;
@@ -270,29 +272,30 @@ int bf_nearandfar(bf_tree_t obs_tree, bf_tree_t src_tree, double alpha, int32_t 
   stack.push_back({0, 0, h0});
   int64_t nf = 0, nn = 0;
   std::vector<Item> kids;
+  auto add_near = [&](const Item& it) {
+    if (near) near->push_back({it.o, it.s});
+    ++nn;
+  };
   while (!stack.empty()) {
     Item it = stack.back();
     stack.pop_back();
     bool lo = to.isleaf(it.o), ls = ts.isleaf(it.s);
     bool adm = is_far(ts, to, it.s, it.o, alpha);
     if (it.h <= minbflvl && !leafcomp) {
-      ++nn;
+      add_near(it);
       continue;
     }
     if (adm) {
       if ((lo || ls) && !leafcomp) {
-        ++nn;
+        add_near(it);
       } else {
-        if (far_obs && far_src && nf < capacity) {
-          far_obs[nf] = it.o;
-          far_src[nf] = it.s;
-        }
+        if (far) far->push_back({it.o, it.s});
         ++nf;
       }
       continue;
     }
     if ((lo && ls) || ((lo || ls) && !leafimbalance)) {
-      ++nn;
+      add_near(it);
       continue;
     }
     kids.clear();
@@ -309,9 +312,56 @@ int bf_nearandfar(bf_tree_t obs_tree, bf_tree_t src_tree, double alpha, int32_t 
   }
   if (n_far) *n_far = nf;
   if (n_near) *n_near = nn;
+}
+
+}  // namespace bfg
+
+extern "C" {
+
+int bf_nearandfar(bf_tree_t obs_tree, bf_tree_t src_tree, double alpha, int32_t minbflvl,
+                  int32_t leafcomp, int32_t leafimbalance, int64_t* far_obs, int64_t* far_src,
+                  int64_t capacity, int64_t* n_far, int64_t* n_near) {
+  if (!obs_tree || !src_tree) {
+    set_error("bf_nearandfar: NULL tree");
+    return BF_EINVAL;
+  }
+  std::vector<std::pair<int64_t, int64_t>> far;
+  int64_t nf = 0, nn = 0;
+  near_far_lists(obs_tree->t, src_tree->t, alpha, minbflvl, leafcomp, leafimbalance,
+                 (far_obs && far_src) ? &far : nullptr, nullptr, &nf, &nn);
+  if (n_far) *n_far = nf;
+  if (n_near) *n_near = nn;
   if (capacity > 0 && nf > capacity) {
     set_error("bf_nearandfar: capacity %lld < %lld far pairs", (long long)capacity, (long long)nf);
     return BF_EINVAL;
+  }
+  for (int64_t i = 0; i < (int64_t)far.size() && i < capacity; ++i) {
+    far_obs[i] = far[i].first;
+    far_src[i] = far[i].second;
+  }
+  return BF_OK;
+}
+
+int bf_near_pairs(bf_tree_t obs_tree, bf_tree_t src_tree, double alpha, int32_t minbflvl,
+                  int32_t leafcomp, int32_t leafimbalance, int64_t* near_obs, int64_t* near_src,
+                  int64_t capacity, int64_t* n_near) {
+  if (!obs_tree || !src_tree) {
+    set_error("bf_near_pairs: NULL tree");
+    return BF_EINVAL;
+  }
+  std::vector<std::pair<int64_t, int64_t>> near;
+  int64_t nn = 0;
+  near_far_lists(obs_tree->t, src_tree->t, alpha, minbflvl, leafcomp, leafimbalance, nullptr,
+                 (near_obs && near_src) ? &near : nullptr, nullptr, &nn);
+  if (n_near) *n_near = nn;
+  if (capacity > 0 && nn > capacity) {
+    set_error("bf_near_pairs: capacity %lld < %lld near pairs", (long long)capacity,
+              (long long)nn);
+    return BF_EINVAL;
+  }
+  for (int64_t i = 0; i < (int64_t)near.size() && i < capacity; ++i) {
+    near_obs[i] = near[i].first;
+    near_src[i] = near[i].second;
   }
   return BF_OK;
 }

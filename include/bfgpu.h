@@ -104,6 +104,13 @@ BF_API int bf_nearandfar(bf_tree_t obs_tree, bf_tree_t src_tree, double alpha,
                          int64_t* far_obs, int64_t* far_src, int64_t capacity,
                          int64_t* n_far, int64_t* n_near);
 
+/* Near pairs of the same traversal (the nearints of intlists.jl:30-217):
+ * (near_obs[i], near_src[i]) in depth-first order; capacity 0 queries *n_near. */
+BF_API int bf_near_pairs(bf_tree_t obs_tree, bf_tree_t src_tree, double alpha,
+                         int32_t minbflvl, int32_t leafcomp, int32_t leafimbalance,
+                         int64_t* near_obs, int64_t* near_src, int64_t capacity,
+                         int64_t* n_near);
+
 /* ------------------------------------------------------------------------
  * Construction on the GPU.
  * Replaces assemble_BF (src/ButterflyFactorization/bfassembly.jl:48-200),
@@ -145,6 +152,20 @@ BF_API int bf_build(bf_ctx_t ctx, const double* obs_xyz, int64_t n_obs, const do
                     int64_t n_src, bf_tree_t obs_tree, bf_tree_t src_tree,
                     const int64_t* far_obs, const int64_t* far_src, int64_t n_far, double k,
                     double tol, const bf_build_opts* opts, bf_op_t* out);
+
+/* Near field of the operator: the near blocks K(values(o), values(s)) of the
+ * given near pairs (PetrovGalerkinBF's BlockSparseMatrix,
+ * src/Matrixassembly/petrovgalerkinbf.jl:57-119), evaluated on the GPU in FP64
+ * for the point Helmholtz kernel (the singular self-term r = 0 is left out:
+ * those entries are zero) and stored as float-float entries, once per
+ * direction.  Afterwards bf_matvec and bf_matvec_noalloc apply near + far in
+ * one device pass (src/matrixalgebra/matrixvector.jl:28-33), forward, adjoint
+ * and transpose.  The point sets and trees are the ones the far field was
+ * built with. */
+BF_API int bf_op_add_near(bf_op_t op, const double* obs_xyz, int64_t n_obs,
+                          const double* src_xyz, int64_t n_src, bf_tree_t obs_tree,
+                          bf_tree_t src_tree, const int64_t* near_obs, const int64_t* near_src,
+                          int64_t n_near, double k);
 
 /* One compression of the GPU build, for parity tests: one call of the
  * PartialQR compressor (src/ButterflyFactorization/compressors.jl:81-165,
@@ -319,6 +340,9 @@ typedef struct {
   double build_upload_seconds;   /* of build_seconds: factor repack + upload      */
   int64_t surrogate_fallbacks;   /* surrogate-seeded compressions that fell back
                                     to the oversampling estimator                 */
+  int64_t near_pairs;            /* near-field blocks (0: far field only)           */
+  int64_t near_entries;          /* stored near-field entries, both directions      */
+  int64_t near_bytes_fwd;        /* algorithmic bytes of one forward near product   */
 } bf_op_stats;
 
 BF_API int bf_op_stats_get(bf_op_t op, bf_op_stats* stats);
@@ -371,6 +395,19 @@ BF_API int bf_op_mixed_info(bf_op_t op, int64_t* factor_bytes, int64_t* workspac
  * *n_tasks.  Used by the tile autotuner and by diagnostics. */
 BF_API int bf_op_task_shapes(bf_op_t op, int64_t* n_tasks, int32_t* stage, int32_t* kind,
                              int32_t* M, int32_t* n);
+
+/* Persisted operators (no reference counterpart: the reference keeps its
+ * factors in memory only and rebuilds them with every assemble_BF,
+ * src/ButterflyFactorization/bfassembly.jl:48-200).  bf_op_save writes the
+ * operator in its packed, device-ready form (level tasks, routing maps,
+ * launch lists, leaf orders, the factor array in its storage, the block list
+ * for bf_op_export_blocks, statistics and rank records) with a format version,
+ * a byte-order mark and 64-bit hashes.  bf_op_load reads such a file onto the
+ * device of ctx without rebuilding: it rejects a wrong magic or truncated /
+ * corrupted file with BF_EINVAL and another format version or byte order with
+ * BF_ENOTSUP, and checks every offset a kernel will follow before upload. */
+BF_API int bf_op_save(bf_op_t op, const char* path);
+BF_API int bf_op_load(bf_ctx_t ctx, const char* path, bf_op_t* out);
 
 BF_API int bf_op_destroy(bf_op_t op);
 

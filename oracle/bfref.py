@@ -707,6 +707,39 @@ def far_matvec(op: FarOperator, x, alpha=1.0, beta=0.0, y=None, adjoint: bool = 
     return y
 
 
+def near_block(kern: HelmholtzKernel, rows, cols) -> np.ndarray:
+    """One near block K(rows, cols) (the blocks of ``petrovgalerkinbf.jl:57-119``) for the
+    point kernel; the singular self-term r = 0 (a point with itself) is left out (zero)."""
+    rows = np.asarray(rows, dtype=np.int64)
+    cols = np.asarray(cols, dtype=np.int64)
+    d = kern.obs[rows][:, None, :] - kern.src[cols][None, :, :]
+    r = np.sqrt(np.einsum("ijk,ijk->ij", d, d))
+    out = np.zeros(r.shape, dtype=np.complex128)
+    nz = r > 0
+    out[nz] = np.exp(-1j * kern.k * r[nz]) / (4.0 * np.pi * r[nz])
+    return out
+
+
+def near_matvec(kern: HelmholtzKernel, tree_o: Tree, tree_s: Tree, near, x, op: str = "N",
+                n_out: int | None = None):
+    """Near-field BlockSparseMatrix product (assembled at ``petrovgalerkinbf.jl:57-119``,
+    applied by ``mul!`` at ``matrixvector.jl:28-33``): y[values(o)] += K_os x[values(s)] over
+    the near pairs; "C" / "T" apply the adjoint / transpose of every block."""
+    if n_out is None:
+        n_out = len(tree_o.perm) if op == "N" else len(tree_s.perm)
+    y = np.zeros(n_out, dtype=np.complex128)
+    for o, s in near:
+        ro, cs = tree_o.values(o), tree_s.values(s)
+        B = near_block(kern, ro, cs)
+        if op == "N":
+            y[ro] += B @ x[cs]
+        elif op == "C":
+            y[cs] += B.conj().T @ x[ro]
+        else:
+            y[cs] += B.T @ x[ro]
+    return y
+
+
 def dense_far(kern, op: FarOperator) -> np.ndarray:
     """Dense far-field matrix: sum over admissible pairs of K[values(NO), values(NS)]."""
     A = np.zeros((op.n_rows, op.n_cols), dtype=np.complex128)

@@ -70,6 +70,23 @@ def test_tree_bit_exact_with_oracle(case):
     fo, nn = bfgpu.nearandfar(b, b, 1.0)
     assert nn == len(near)
     assert np.array_equal(np.asarray(far, np.int64).reshape(-1, 2), fo)
+    assert np.array_equal(np.asarray(near, np.int64).reshape(-1, 2), bfgpu.near_pairs(b, b, 1.0))
+
+
+@pytest.mark.parametrize("opts", [dict(leafcomp=False), dict(leafimbalance=False),
+                                  dict(minbflvl=2, leafcomp=False)])
+def test_near_and_far_lists_options(opts):
+    """Near and far pairs of the dual traversal under the non-default options
+    (intlists.jl:30-217), unbalanced trees: bit-exact with the oracle."""
+    obs, src = G.plane_pair(3000, 7, z_obs=0.2)
+    a_o, a_s = O.build_tree(obs, max_points=12), O.build_tree(src, max_points=60)
+    b_o, b_s = bfgpu.Tree.build(obs, max_points=12), bfgpu.Tree.build(src, max_points=60)
+    far, near = O.nearandfar(a_o, a_s, 1.0, **opts)
+    fo, nn = bfgpu.nearandfar(b_o, b_s, 1.0, **opts)
+    assert np.array_equal(np.asarray(far, np.int64).reshape(-1, 2), fo)
+    assert np.array_equal(np.asarray(near, np.int64).reshape(-1, 2),
+                          bfgpu.near_pairs(b_o, b_s, 1.0, **opts))
+    assert nn == len(near) > 0
 
 
 def test_tree_from_arrays_roundtrip():
