@@ -102,7 +102,7 @@ def test_alpha_beta_multi_rhs_and_device(sphere, ctx):
 def test_non_leaf_near_pairs_unbalanced_trees(ctx, opts):
     """Plane pair 0.2 apart, observer leaves <= 12 points, source leaves <= 60: near pairs
     with non-leaf nodes, split over the leaves below them."""
-    obs, src = G.plane_pair(1500, 7, z_obs=0.2)
+    obs, src = G.plane_pair(3000, 7, z_obs=0.2)
     case = make_case(ctx, obs, src, 2 * math.pi / 0.25, max_o=12, max_s=60, **opts)
     assert any(not (case["to"].isleaf(o) and case["ts"].isleaf(s)) for o, s in case["near"])
     for d in ("N", "C", "T"):
