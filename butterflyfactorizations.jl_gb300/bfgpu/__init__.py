@@ -34,7 +34,7 @@ from ._lib import (BF_OP_C, BF_OP_N, BF_OP_T, BF_PTR_DEVICE, BF_PTR_HOST, BF_STO
                    check, load)
 
 __all__ = ["Tree", "Context", "Operator", "nearandfar", "assemble_BF", "PetrovGalerkinBF",
-           "import_blocks", "load_operator", "compress_block", "near_pairs", "mul", "BFError",
+           "import_blocks", "load_operator", "compress_block", "near_pairs", "nearandfar_gpu", "mul", "BFError",
            "load"]
 
 
@@ -77,6 +77,20 @@ class Tree:
                                 -1 if max_points is None else int(max_points),
                                 -1 if max_depth is None else int(max_depth), C.byref(h)),
               "bf_tree_build")
+        return cls(h.value, pts)
+
+    @classmethod
+    def build_gpu(cls, points, max_points: int | None = None, max_depth: int | None = None,
+                  ctx: "Context | None" = None):
+        """The same tree as ``build``, with the point partitioning on the GPU."""
+        lib = load()
+        ctx = ctx or default_context()
+        pts = np.ascontiguousarray(points, dtype=np.float64)
+        h = C.c_void_p()
+        check(lib.bf_tree_build_gpu(ctx._h, _p(pts, C.c_double), pts.shape[0],
+                                    -1 if max_points is None else int(max_points),
+                                    -1 if max_depth is None else int(max_depth), C.byref(h)),
+              "bf_tree_build_gpu")
         return cls(h.value, pts)
 
     @property
@@ -135,6 +149,26 @@ def near_pairs(tree_o: Tree, tree_s: Tree, alpha: float = 1.0, minbflvl: int = 3
     check(lib.bf_near_pairs(*args, _p(fo, C.c_int64), _p(fs, C.c_int64), max(nn.value, 1),
                             C.byref(nn)), "bf_near_pairs")
     return np.stack([fo[:nn.value], fs[:nn.value]], axis=1)
+
+
+def nearandfar_gpu(tree_o: Tree, tree_s: Tree, alpha: float = 1.0, minbflvl: int = 3,
+                   leafcomp: bool = True, leafimbalance: bool = True, ctx=None):
+    """Far and near pairs, (n, 2) arrays each, traversed on the GPU (same order as
+    ``nearandfar`` / ``near_pairs``)."""
+    lib = load()
+    ctx = ctx or default_context()
+    nf, nn = C.c_int64(), C.c_int64()
+    args = (ctx._h, tree_o._h, tree_s._h, float(alpha), int(minbflvl), int(leafcomp),
+            int(leafimbalance))
+    check(lib.bf_nearandfar_gpu(*args, None, None, 0, None, None, 0, C.byref(nf), C.byref(nn)),
+          "bf_nearandfar_gpu")
+    a = [np.zeros(max(v, 1), np.int64) for v in (nf.value, nf.value, nn.value, nn.value)]
+    check(lib.bf_nearandfar_gpu(*args, _p(a[0], C.c_int64), _p(a[1], C.c_int64), len(a[0]),
+                                _p(a[2], C.c_int64), _p(a[3], C.c_int64), len(a[2]),
+                                C.byref(nf), C.byref(nn)), "bf_nearandfar_gpu")
+    far = np.stack([a[0][:nf.value], a[1][:nf.value]], axis=1)
+    near = np.stack([a[2][:nn.value], a[3][:nn.value]], axis=1)
+    return far, near
 
 
 class Context:

@@ -35,7 +35,10 @@ def _cmd(src: str, obj: str):
     if src.endswith(".cu"):
         return [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                 "-Xptxas", "-warn-spills", "-I", INCLUDE, "-I", CSRC, "-c", path, "-o", obj]
-    return ["g++", "-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-Wall",
+    # -ffp-contract=off: no fused multiply-adds in host code, so the FP64 tests of the
+    # tree traversal round the same on x86-64, aarch64 and in the device version
+    return ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-fvisibility=hidden",
+            "-Wall",
             "-Wno-unused-function", "-I", INCLUDE, "-I", CSRC, "-I",
             os.path.join(CUDA, "include"), "-fopenmp", "-c", path, "-o", obj]
 

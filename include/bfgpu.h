@@ -104,6 +104,23 @@ BF_API int bf_nearandfar(bf_tree_t obs_tree, bf_tree_t src_tree, double alpha,
                          int64_t* far_obs, int64_t* far_src, int64_t capacity,
                          int64_t* n_far, int64_t* n_near);
 
+/* The same tree and interaction lists, built on the GPU (the reference builds
+ * its trees in H2Trees, ext/BFH2Trees/bisection_tree.jl:27-145, and its lists
+ * in intlists.jl:30-217, on the host).  bf_tree_build_gpu returns a tree
+ * identical, node for node and point for point, to bf_tree_build's: the device
+ * partitions the points level by level, the host numbers the nodes.
+ * bf_nearandfar_gpu returns the far and near pairs of bf_nearandfar /
+ * bf_near_pairs in the same depth-first order (level-synchronous traversal on
+ * the device, outputs placed by their depth-first keys); capacities 0 query
+ * *n_far / *n_near.  Traversals deeper than 21 levels return BF_ENOTSUP. */
+BF_API int bf_tree_build_gpu(bf_ctx_t ctx, const double* xyz, int64_t n_points,
+                             int32_t max_points, int32_t max_depth, bf_tree_t* out);
+BF_API int bf_nearandfar_gpu(bf_ctx_t ctx, bf_tree_t obs_tree, bf_tree_t src_tree, double alpha,
+                             int32_t minbflvl, int32_t leafcomp, int32_t leafimbalance,
+                             int64_t* far_obs, int64_t* far_src, int64_t far_capacity,
+                             int64_t* near_obs, int64_t* near_src, int64_t near_capacity,
+                             int64_t* n_far, int64_t* n_near);
+
 /* Near pairs of the same traversal (the nearints of intlists.jl:30-217):
  * (near_obs[i], near_src[i]) in depth-first order; capacity 0 queries *n_near. */
 BF_API int bf_near_pairs(bf_tree_t obs_tree, bf_tree_t src_tree, double alpha,
