@@ -308,9 +308,10 @@ struct NearField {
   std::vector<DTask> tasks;
   int64_t n_fwd = 0;
   std::vector<int32_t> maps;  // routing entries (workspace entries)
-  // launch lists: small tasks (M <= 32) and tall row panels ((task, row0)
-  // pairs), forward then adjoint; list_begin[c] .. list_begin[c + 1]
-  enum { N_SMALL_F = 0, N_TALL_F, N_SMALL_A, N_TALL_A, N_NCLASS };
+  // launch lists: tall row panels ((task, row0) pairs, read as int2: both
+  // tall lists come first, so they start at even offsets) and small tasks
+  // (M <= 32), forward and adjoint; list_begin[c] .. list_begin[c + 1]
+  enum { N_TALL_F = 0, N_TALL_A, N_SMALL_F, N_SMALL_A, N_NCLASS };
   std::vector<int32_t> lists;
   int64_t list_begin[N_NCLASS + 1] = {};
   int64_t a_entries = 0;      // float-float entries, both directions

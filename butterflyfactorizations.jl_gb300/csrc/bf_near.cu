@@ -335,12 +335,18 @@ extern "C" int bf_op_add_near(bf_op_t h, const double* obs_xyz, int64_t n_obs,
     N.alg_bytes_fwd = fwd_alg;
     N.fwd_covered = covered_f == p.n_rows ? 1 : 0;
     N.adj_covered = covered_a == p.n_cols ? 1 : 0;
-    const std::vector<int32_t>* cls[NearField::N_NCLASS] = {&small_f, &tall_f, &small_a,
-                                                             &tall_a};
+    const std::vector<int32_t>* cls[NearField::N_NCLASS];
+    cls[NearField::N_TALL_F] = &tall_f;
+    cls[NearField::N_TALL_A] = &tall_a;
+    cls[NearField::N_SMALL_F] = &small_f;
+    cls[NearField::N_SMALL_A] = &small_a;
     for (int c = 0; c < NearField::N_NCLASS; ++c) {
       N.list_begin[c] = (int64_t)N.lists.size();
       N.lists.insert(N.lists.end(), cls[c]->begin(), cls[c]->end());
     }
+    // tall items are read as int2: their lists must start at even offsets
+    if ((N.list_begin[NearField::N_TALL_F] | N.list_begin[NearField::N_TALL_A]) & 1)
+      throw std::length_error("near field: tall list misaligned");
     N.list_begin[NearField::N_NCLASS] = (int64_t)N.lists.size();
     if (N.a_entries >= ((int64_t)1 << 40)) throw std::length_error("near field too large");
     // device: entries (evaluated here), tasks, maps, lists, the larger workspace

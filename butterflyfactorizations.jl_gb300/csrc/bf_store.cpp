@@ -161,8 +161,9 @@ int validate_near(const Operator& op) {
     const int64_t b = N.list_begin[c], e = N.list_begin[c + 1];
     if (e < b || e > nl) return bad("list range");
     const bool tall = c == NearField::N_TALL_F || c == NearField::N_TALL_A;
-    const bool adj = c >= NearField::N_SMALL_A;
-    if (tall && ((e - b) & 1)) return bad("tall list");
+    const bool adj = c == NearField::N_TALL_A || c == NearField::N_SMALL_A;
+    // tall items are (task, row0) pairs read as int2: even start and length
+    if (tall && (((e - b) & 1) || (b & 1))) return bad("tall list");
     for (int64_t q = b; q < e; ++q) {
       const int32_t v = N.lists[q];
       if (tall && ((q - b) & 1)) {
@@ -212,6 +213,8 @@ int validate(const Operator& op) {
     if ((int64_t)b.size() != ns + 1) return bad("launch list bounds");
     for (int64_t s = 0; s < ns; ++s) {
       if (b[s] < 0 || b[s + 1] < b[s] || b[s + 1] > nl) return bad("launch list range");
+      // tall items are (task, row0) pairs read as int2: even start and length
+      if (c == Plan::L_TALL && ((b[s] | (b[s + 1] - b[s])) & 1)) return bad("tall list");
       for (int64_t q = b[s]; q < b[s + 1]; ++q) {
         const bool row = c == Plan::L_TALL && ((q - b[s]) & 1);  // tall items: (task, row0)
         const int32_t v = p.lists[q];
