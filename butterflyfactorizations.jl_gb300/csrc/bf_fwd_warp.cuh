@@ -10,8 +10,7 @@
 // kernels (bf_batch.cu).  The tall, small and copy routines take NR
 // right-hand sides at once: workspace entry e of right-hand side q is
 // ws[e*S + q] (S >= NR; the single-vector path has NR = S = 1), and every
-// factor entry loaded is applied to all NR of them from registers.  CONJ
-// multiplies by the conjugated entries (the near field's adjoint).  Blackwell's paired FP32
+// factor entry loaded is applied to all NR of them from registers.  Blackwell's paired FP32
 // instructions (__ffma2_rn and relatives) were measured slower here: a pair
 // costs the FMA pipes as much as two scalar operations, and the operand
 // broadcasts they need add instructions.
@@ -66,7 +65,7 @@ __device__ __forceinline__ void stage_cols(const DTask& t, const int32_t* __rest
 // loaded at once under predicates, so a warp waits on few serial latencies.
 // (Keeping two batches in flight instead was measured slower: the extra
 // registers cost more occupancy than the overlap gained.)
-template <typename FT, int NR = 1, bool CONJ = false>
+template <typename FT, int NR = 1>
 __device__ __forceinline__ void warp_tall(const DTask& t, int r0, const FT* __restrict__ A,
                                           const int32_t* __restrict__ maps,
                                           float4* __restrict__ ws, float4* __restrict__ xw,
@@ -107,12 +106,7 @@ __device__ __forceinline__ void warp_tall(const DTask& t, int r0, const FT* __re
           for (int r = 0; r < NR; ++r) {
             const float4 xc = xw[(j + c) * NR + r];
 #pragma unroll
-            for (int q = 0; q < TALL_RPL; ++q) {
-              if constexpr (CONJ)
-                cdf_mac_conj(acc[q][r], v[c][q], xc);
-              else
-                cdf_mac(acc[q][r], v[c][q], xc);
-            }
+            for (int q = 0; q < TALL_RPL; ++q) cdf_mac(acc[q][r], v[c][q], xc);
           }
         }
     };
@@ -209,7 +203,7 @@ __device__ __forceinline__ void warp_flat(const DTask& t, const FT* __restrict__
 
 // M <= 32: G = 32/M lane groups walk interleaved columns (one warp load reads
 // G*M contiguous entries); the groups meet in shared memory at the end.
-template <typename FT, int NR = 1, bool CONJ = false>
+template <typename FT, int NR = 1>
 __device__ __forceinline__ void warp_small(const DTask& t, const FT* __restrict__ A,
                                            const int32_t* __restrict__ maps,
                                            float4* __restrict__ ws, float4* __restrict__ xw,
@@ -246,12 +240,7 @@ __device__ __forceinline__ void warp_small(const DTask& t, const FT* __restrict_
         const int j = g + (k + u) * G;
         if (active && j < nb) {
 #pragma unroll
-          for (int r = 0; r < NR; ++r) {
-            if constexpr (CONJ)
-              cdf_mac_conj(acc[r], v[u], xw[j * NR + r]);
-            else
-              cdf_mac(acc[r], v[u], xw[j * NR + r]);
-          }
+          for (int r = 0; r < NR; ++r) cdf_mac(acc[r], v[u], xw[j * NR + r]);
         }
       }
     };

@@ -308,26 +308,32 @@ struct NearField {
   std::vector<DTask> tasks;
   int64_t n_fwd = 0;
   std::vector<int32_t> maps;  // routing entries (workspace entries)
+  // point ids, indexed like maps: the kernels read a column's input x[pts[j]]
+  // in FP64 straight from the caller's vector
+  std::vector<int32_t> pts;
   // launch lists: tall row panels ((task, row0) pairs, read as int2: both
   // tall lists come first, so they start at even offsets) and small tasks
   // (M <= 32), forward and adjoint; list_begin[c] .. list_begin[c + 1]
   enum { N_TALL_F = 0, N_TALL_A, N_SMALL_F, N_SMALL_A, N_NCLASS };
   std::vector<int32_t> lists;
   int64_t list_begin[N_NCLASS + 1] = {};
-  int64_t a_entries = 0;      // float-float entries, both directions
+  int64_t a_entries = 0;      // complex FP64 entries, both directions
   int64_t ny_off = 0, nx_off = 0;
   int32_t fwd_covered = 0, adj_covered = 0;
   int64_t n_pairs = 0;
   int64_t alg_bytes_fwd = 0;  // bytes of one forward near product
-  float4* d_A = nullptr;
+  double2* d_A = nullptr;
   DTask* d_tasks = nullptr;
   int32_t* d_maps = nullptr;
+  int32_t* d_pts = nullptr;
   int32_t* d_lists = nullptr;
 };
 void near_free(NearField* nf);
 int near_upload(NearField& nf);  // tasks, maps, lists (the entries are uploaded by their producer)
-// near-field launches of one matvec into ws (after the far levels, before the combine)
-int near_stage(const struct Operator& op, int trans, cudaStream_t st, float4* ws, int64_t* nk);
+// near-field launches of one matvec: inputs from x (device, the caller's
+// vector: n_cols entries forward, n_rows adjoint), results into ws's near region
+int near_stage(const struct Operator& op, int trans, cudaStream_t st, const double2* x,
+               float4* ws, int64_t* nk);
 // y_c += alpha * near(op) x_c for nrhs columns (device pointers), through op's workspace
 int near_apply_columns(struct Operator& op, int trans, int64_t nrhs, const double2* x,
                        int64_t lx, double2* y, int64_t ly, double2 alpha, cudaStream_t st);

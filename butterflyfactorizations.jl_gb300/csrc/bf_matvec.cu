@@ -439,7 +439,7 @@ static int matvec_one(Operator& op, int trans, const double2* x, double2* y, dou
   for (int64_t k = 0; k < ns; ++k) BF_TRY(launch_stage(op, fwd ? k : ns - 1 - k, trans, st, ws, nullptr));
   int64_t near_off = -1;
   if (op.near) {  // near + far in one pass (matrixvector.jl:28-33)
-    BF_TRY(near_stage(op, trans, st, ws, nullptr));
+    BF_TRY(near_stage(op, trans, st, x, ws, nullptr));
     near_off = fwd ? op.near->ny_off : op.near->nx_off;
   }
   combine_kernel<<<grid_for(nout, 256), 256, 0, st>>>(y, nout, ws, out_off, near_off, alpha, beta,

@@ -8,10 +8,17 @@
 // the blocks of every near pair whose observer node is the leaf or one of its
 // ancestors, side by side (the P-stage shape: few rows, many columns), so every
 // output entry has one writer; the adjoint gets its own tasks, one per source
-// leaf with the transposed blocks.  The entries are evaluated once, on the
-// GPU, in FP64 (k*r, sincos, 1/(4 pi r)) and stored as float-float pairs, so
-// the near product is FP64-accurate like the far one.  The point kernel is
-// singular at r = 0; those entries (a point with itself) are zero.
+// leaf with the transposed blocks.
+//
+// Arithmetic is FP64 throughout, as in the reference: the entries are
+// evaluated once on the GPU (k*r, sincos, 1/(4 pi r)) and stored as complex
+// FP64 (16 B, the bytes of a float-float entry), the inputs are read in FP64
+// straight from the caller's vector by point id, and the sums run on the FP64
+// FMA pipe.  Near rows sum thousands of large entries of opposing phase, where
+// the 48 bits of float-float storage cost up to ~1e-12 of relative accuracy;
+// at 8 flop per 16-byte entry the FP64 pipe of GB300 (~1.2 TFLOP/s) keeps
+// about the speed of the float-float kernels.  The point kernel is singular at
+// r = 0; those entries (a point with itself) are zero.
 #include <algorithm>
 #include <memory>
 #include <stdexcept>
@@ -36,7 +43,7 @@ struct alignas(16) NearEval {
 __global__ void near_eval_kernel(const NearEval* __restrict__ ev, const double* __restrict__ obs,
                                  const double* __restrict__ src, const int32_t* __restrict__ pts_r,
                                  const int32_t* __restrict__ pts_c, double k,
-                                 float4* __restrict__ A) {
+                                 double2* __restrict__ A) {
   const NearEval e = ev[blockIdx.x];
   const long long tot = (long long)e.M * e.n;
   for (long long q = threadIdx.x; q < tot; q += blockDim.x) {
@@ -54,21 +61,7 @@ __global__ void near_eval_kernel(const NearEval* __restrict__ ev, const double* 
       re = cs * inv;
       im = -sn * inv;
     }
-    const float2 hr = df_split(re), hi = df_split(im);
-    A[e.a_off + q] = make_float4(hr.x, hr.y, hi.x, hi.y);
-  }
-}
-
-// one right-hand side into the input region of the workspace (float-float,
-// leaf order): ws[off + q] = x[perm[q]]
-__global__ void near_split_kernel(const double2* __restrict__ x, int64_t n,
-                                  float4* __restrict__ ws, int64_t off,
-                                  const int32_t* __restrict__ perm) {
-  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
-       q += (int64_t)gridDim.x * blockDim.x) {
-    const double2 v = x[perm[q]];
-    const float2 re = df_split(v.x), im = df_split(v.y);
-    ws[off + q] = make_float4(re.x, re.y, im.x, im.y);
+    A[e.a_off + q] = make_double2(re, im);
   }
 }
 
@@ -86,46 +79,129 @@ __global__ void near_add_kernel(double2* __restrict__ y, int64_t n, const float4
   }
 }
 
+// acc += a * v, or conj(a) * v, in FP64
+template <bool CONJ>
+__device__ __forceinline__ void zmac(double2& acc, const double2 a, const double2 v) {
+  const double ai = CONJ ? -a.y : a.y;
+  acc.x = fma(a.x, v.x, acc.x);
+  acc.x = fma(-ai, v.y, acc.x);
+  acc.y = fma(a.x, v.y, acc.y);
+  acc.y = fma(ai, v.x, acc.y);
+}
+
+__device__ __forceinline__ float4 split_z(const double2 v) {
+  const float2 re = df_split(v.x), im = df_split(v.y);
+  return make_float4(re.x, re.y, im.x, im.y);
+}
+
+constexpr int NX = 256;  // input entries staged per warp and pass
+constexpr int NLU = 4;   // factor loads in flight per lane
+
+// Task with M <= 32 rows, one warp: G = 32/M lane groups walk interleaved
+// columns (one warp load covers G*M contiguous entries), then meet in shared
+// memory.  Inputs x[point of column j] are staged per pass; the result of
+// row i goes to ws[rmap[i]] as a float-float entry.
 template <bool CONJ>
 __global__ void __launch_bounds__(FW_WARPS * 32) near_small_kernel(
     const int32_t* __restrict__ tlist, int n_tasks, const DTask* __restrict__ tasks,
-    const float4* __restrict__ A, const int32_t* __restrict__ maps, float4* __restrict__ ws) {
-  __shared__ float4 xs[FW_WARPS][FW_XB];
-  const int warp = threadIdx.x >> 5;
+    const double2* __restrict__ A, const int32_t* __restrict__ maps,
+    const int32_t* __restrict__ pts, const double2* __restrict__ x, float4* __restrict__ ws) {
+  __shared__ double2 xs[FW_WARPS][NX];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ti = blockIdx.x * FW_WARPS + warp;
   if (ti >= n_tasks) return;
   const DTask t = tasks[tlist[ti]];
-  warp_small<float4, 1, CONJ>(t, A, maps, ws, xs[warp]);
+  const int M = t.M, n = t.n;
+  const int G = 32 / M, g = lane / M, i = lane - g * M;
+  const bool active = g < G;
+  const int32_t* __restrict__ cpt = pts + t.cmap_off;
+  double2* xw = xs[warp];
+  double2 acc = make_double2(0.0, 0.0);
+  for (int cb = 0; cb < n; cb += NX) {
+    const int nb = min(NX, n - cb);
+    for (int j = lane; j < nb; j += 32) xw[j] = x[cpt[cb + j]];
+    __syncwarp();
+    if (active) {
+      const double2* __restrict__ ap = A + t.a_off + (size_t)(cb + g) * M + i;
+      const size_t step = (size_t)G * M;
+      int j = g;
+      for (; j + (NLU - 1) * G < nb; j += NLU * G) {
+        double2 a[NLU];
+#pragma unroll
+        for (int u = 0; u < NLU; ++u) a[u] = __ldg(ap + u * step);
+#pragma unroll
+        for (int u = 0; u < NLU; ++u) zmac<CONJ>(acc, a[u], xw[j + u * G]);
+        ap += NLU * step;
+      }
+      for (; j < nb; j += G, ap += step) zmac<CONJ>(acc, __ldg(ap), xw[j]);
+    }
+    __syncwarp();
+  }
+  if (G > 1) {
+    xw[lane] = acc;  // the staging buffer holds the groups' partial sums
+    __syncwarp();
+    if (active && g == 0) {
+      for (int q = 1; q < G; ++q) {
+        const double2 v = xw[q * M + i];
+        acc.x += v.x;
+        acc.y += v.y;
+      }
+    }
+  }
+  if (active && g == 0) ws[maps[t.rmap_off + i]] = split_z(acc);
 }
 
+// Task with M > 32 rows: one warp per 64-row panel (item = task, first row),
+// two rows per lane, coalesced loads down the columns.
 template <bool CONJ>
 __global__ void __launch_bounds__(FW_WARPS * 32) near_tall_kernel(
     const int2* __restrict__ items, int n_items, const DTask* __restrict__ tasks,
-    const float4* __restrict__ A, const int32_t* __restrict__ maps, float4* __restrict__ ws) {
-  __shared__ float4 xs[FW_WARPS][FW_XB];
-  const int warp = threadIdx.x >> 5;
+    const double2* __restrict__ A, const int32_t* __restrict__ maps,
+    const int32_t* __restrict__ pts, const double2* __restrict__ x, float4* __restrict__ ws) {
+  __shared__ double2 xs[FW_WARPS][NX];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int item = blockIdx.x * FW_WARPS + warp;
   if (item >= n_items) return;
   const int2 it = items[item];
   const DTask t = tasks[it.x];
-  warp_tall<float4, 1, CONJ>(t, it.y, A, maps, ws, xs[warp]);
+  const int M = t.M, n = t.n, r0 = it.y;
+  if (r0 >= M) return;
+  const int32_t* __restrict__ cpt = pts + t.cmap_off;
+  double2* xw = xs[warp];
+  const bool act0 = r0 + lane < M, act1 = r0 + lane + 32 < M;
+  double2 acc0 = make_double2(0.0, 0.0), acc1 = make_double2(0.0, 0.0);
+  for (int cb = 0; cb < n; cb += NX) {
+    const int nb = min(NX, n - cb);
+    for (int j = lane; j < nb; j += 32) xw[j] = x[cpt[cb + j]];
+    __syncwarp();
+    const double2* __restrict__ ap = A + t.a_off + (size_t)cb * M + r0 + lane;
+#pragma unroll 4
+    for (int j = 0; j < nb; ++j, ap += M) {
+      const double2 v = xw[j];
+      if (act0) zmac<CONJ>(acc0, __ldg(ap), v);
+      if (act1) zmac<CONJ>(acc1, __ldg(ap + 32), v);
+    }
+    __syncwarp();
+  }
+  if (act0) ws[maps[t.rmap_off + r0 + lane]] = split_z(acc0);
+  if (act1) ws[maps[t.rmap_off + r0 + lane + 32]] = split_z(acc1);
 }
 
 template <bool CONJ>
-int launch_near(const NearField& nf, int small, int tall, cudaStream_t st, float4* ws,
-                int64_t* nk) {
+int launch_near(const NearField& nf, int small, int tall, cudaStream_t st, const double2* x,
+                float4* ws, int64_t* nk) {
   const unsigned WT = FW_WARPS * 32;
   int64_t b = nf.list_begin[small], n = nf.list_begin[small + 1] - b;
   if (n > 0) {
     near_small_kernel<CONJ><<<(unsigned)((n + FW_WARPS - 1) / FW_WARPS), WT, 0, st>>>(
-        nf.d_lists + b, (int)n, nf.d_tasks, nf.d_A, nf.d_maps, ws);
+        nf.d_lists + b, (int)n, nf.d_tasks, nf.d_A, nf.d_maps, nf.d_pts, x, ws);
     if (nk) ++*nk;
   }
   b = nf.list_begin[tall];
   n = (nf.list_begin[tall + 1] - b) / 2;
   if (n > 0) {
     near_tall_kernel<CONJ><<<(unsigned)((n + FW_WARPS - 1) / FW_WARPS), WT, 0, st>>>(
-        (const int2*)(nf.d_lists + b), (int)n, nf.d_tasks, nf.d_A, nf.d_maps, ws);
+        (const int2*)(nf.d_lists + b), (int)n, nf.d_tasks, nf.d_A, nf.d_maps, nf.d_pts, x, ws);
     if (nk) ++*nk;
   }
   BF_TRY_CUDA(cudaGetLastError());
@@ -148,6 +224,7 @@ void near_free(NearField* nf) {
   if (nf->d_A) cudaFree(nf->d_A);
   if (nf->d_tasks) cudaFree(nf->d_tasks);
   if (nf->d_maps) cudaFree(nf->d_maps);
+  if (nf->d_pts) cudaFree(nf->d_pts);
   if (nf->d_lists) cudaFree(nf->d_lists);
   delete nf;
 }
@@ -159,25 +236,29 @@ int near_upload(NearField& nf) {
   BF_TRY_CUDA(cudaMalloc(&nf.d_maps, std::max<size_t>(1, nf.maps.size()) * sizeof(int32_t)));
   BF_TRY_CUDA(cudaMemcpy(nf.d_maps, nf.maps.data(), nf.maps.size() * sizeof(int32_t),
                          cudaMemcpyHostToDevice));
+  BF_TRY_CUDA(cudaMalloc(&nf.d_pts, std::max<size_t>(1, nf.pts.size()) * sizeof(int32_t)));
+  BF_TRY_CUDA(cudaMemcpy(nf.d_pts, nf.pts.data(), nf.pts.size() * sizeof(int32_t),
+                         cudaMemcpyHostToDevice));
   BF_TRY_CUDA(cudaMalloc(&nf.d_lists, std::max<size_t>(1, nf.lists.size()) * sizeof(int32_t)));
   BF_TRY_CUDA(cudaMemcpy(nf.d_lists, nf.lists.data(), nf.lists.size() * sizeof(int32_t),
                          cudaMemcpyHostToDevice));
   return BF_OK;
 }
 
-int near_stage(const Operator& op, int trans, cudaStream_t st, float4* ws, int64_t* nk) {
+int near_stage(const Operator& op, int trans, cudaStream_t st, const double2* x, float4* ws,
+               int64_t* nk) {
   const NearField& nf = *op.near;
   const Plan& p = op.plan;
   if (trans == BF_OP_N) {
     if (!nf.fwd_covered)
       BF_TRY_CUDA(cudaMemsetAsync(ws + nf.ny_off, 0, (size_t)p.n_rows * sizeof(float4), st));
-    return launch_near<false>(nf, NearField::N_SMALL_F, NearField::N_TALL_F, st, ws, nk);
+    return launch_near<false>(nf, NearField::N_SMALL_F, NearField::N_TALL_F, st, x, ws, nk);
   }
   if (!nf.adj_covered)
     BF_TRY_CUDA(cudaMemsetAsync(ws + nf.nx_off, 0, (size_t)p.n_cols * sizeof(float4), st));
   if (trans == BF_OP_C)
-    return launch_near<true>(nf, NearField::N_SMALL_A, NearField::N_TALL_A, st, ws, nk);
-  return launch_near<false>(nf, NearField::N_SMALL_A, NearField::N_TALL_A, st, ws, nk);
+    return launch_near<true>(nf, NearField::N_SMALL_A, NearField::N_TALL_A, st, x, ws, nk);
+  return launch_near<false>(nf, NearField::N_SMALL_A, NearField::N_TALL_A, st, x, ws, nk);
 }
 
 // y_c += alpha * near(op) x_c for every column, on top of a far-field result
@@ -186,15 +267,11 @@ int near_apply_columns(Operator& op, int trans, int64_t nrhs, const double2* x, 
                        double2* y, int64_t ly, double2 alpha, cudaStream_t st) {
   const Plan& p = op.plan;
   const bool fwd = trans == BF_OP_N;
-  const int64_t nin = fwd ? p.n_cols : p.n_rows, nout = fwd ? p.n_rows : p.n_cols;
-  const int64_t in_off = fwd ? p.xg_off : p.yg_off;
+  const int64_t nout = fwd ? p.n_rows : p.n_cols;
   const int64_t out_off = fwd ? op.near->ny_off : op.near->nx_off;
-  const unsigned gi = (unsigned)std::max<int64_t>(1, std::min<int64_t>((nin + 255) / 256, 2432));
   const unsigned go = (unsigned)std::max<int64_t>(1, std::min<int64_t>((nout + 255) / 256, 2432));
   for (int64_t c = 0; c < nrhs; ++c) {
-    near_split_kernel<<<gi, 256, 0, st>>>(x + c * lx, nin, op.d_ws, in_off,
-                                          fwd ? op.d_xperm : op.d_yperm);
-    BF_TRY(near_stage(op, trans, st, op.d_ws, nullptr));
+    BF_TRY(near_stage(op, trans, st, x + c * lx, op.d_ws, nullptr));
     near_add_kernel<<<go, 256, 0, st>>>(y + c * ly, nout, op.d_ws, out_off, alpha,
                                         fwd ? op.d_yperm : op.d_xperm);
   }
@@ -292,6 +369,7 @@ extern "C" int bf_op_add_near(bf_op_t h, const double* obs_xyz, int64_t n_obs,
         for (int64_t i = 0; i < M; ++i) {
           const int64_t e = rbase_off + rpos[rv[i]];
           N.maps.push_back((int32_t)e);
+          N.pts.push_back((int32_t)rv[i]);
           if (e != rbase_off + rpos[rv[0]] + i) contig = false;
         }
         t.rbase = contig ? (int)(rbase_off + rpos[rv[0]]) : -1;
@@ -308,6 +386,7 @@ extern "C" int bf_op_add_near(bf_op_t h, const double* obs_xyz, int64_t n_obs,
           const int64_t* cv = ct.vals(c);
           for (int64_t j = 0; j < ct.nvals(c); ++j) {
             N.maps.push_back((int32_t)(cbase_off + cpos[cv[j]]));
+            N.pts.push_back((int32_t)cv[j]);
             pts_c.push_back((int32_t)cv[j]);
           }
         }
@@ -376,7 +455,7 @@ extern "C" int bf_op_add_near(bf_op_t h, const double* obs_xyz, int64_t n_obs,
     tmp.p.push_back(d_pr);
     BF_TRY(dev(pts_c.size() * sizeof(int32_t), &d_pc));
     tmp.p.push_back(d_pc);
-    BF_TRY(dev((size_t)N.a_entries * sizeof(float4), (void**)&N.d_A));
+    BF_TRY(dev((size_t)N.a_entries * sizeof(double2), (void**)&N.d_A));
     BF_TRY_CUDA(cudaMemcpy(d_obs, obs_xyz, 3 * (size_t)n_obs * sizeof(double),
                            cudaMemcpyHostToDevice));
     BF_TRY_CUDA(cudaMemcpy(d_src, src_xyz, 3 * (size_t)n_src * sizeof(double),

@@ -155,6 +155,16 @@ int validate_near(const Operator& op) {
   }
   for (int32_t v : N.maps)
     if (v < 0 || v >= p.ws_entries) return bad("routing map entry");
+  if (N.pts.size() != N.maps.size()) return bad("point ids");
+  // the kernels read x[pts[column]]: source points forward, observer points adjoint
+  for (int64_t q = 0; q < nt; ++q) {
+    const DTask& t = N.tasks[q];
+    const int64_t lim = q < N.n_fwd ? p.n_cols : p.n_rows;
+    for (int64_t j = 0; j < t.n; ++j) {
+      const int32_t v = N.pts[t.cmap_off + j];
+      if (v < 0 || v >= lim) return bad("point id");
+    }
+  }
   const int64_t nl = (int64_t)N.lists.size();
   if (N.list_begin[0] != 0 || N.list_begin[NearField::N_NCLASS] != nl) return bad("lists");
   for (int c = 0; c < NearField::N_NCLASS; ++c) {
@@ -314,6 +324,7 @@ extern "C" int bf_op_save(bf_op_t h, const char* path) {
       w.pod(ns);
       w.vec(N.tasks);
       w.vec(N.maps);
+      w.vec(N.pts);
       w.vec(N.lists);
     }
     const uint64_t head_hash = w.h;
@@ -334,7 +345,7 @@ extern "C" int bf_op_save(bf_op_t h, const char* path) {
       return BF_OK;
     };
     BF_TRY(put(dA, (uint64_t)p.a_entries * p.fac_bytes));
-    if (op.near) BF_TRY(put(op.near->d_A, (uint64_t)op.near->a_entries * sizeof(float4)));
+    if (op.near) BF_TRY(put(op.near->d_A, (uint64_t)op.near->a_entries * sizeof(double2)));
     w.raw(&head_hash, 8, false);
     w.raw(END_MAGIC, 8, false);
     if (!w.ok || std::fflush(f.get()) != 0) {
@@ -451,6 +462,7 @@ extern "C" int bf_op_load(bf_ctx_t ctx, const char* path, bf_op_t* out) {
       N.adj_covered = ns.adj_covered;
       r.vec(N.tasks);
       r.vec(N.maps);
+      r.vec(N.pts);
       r.vec(N.lists);
     }
     const uint64_t head_hash = r.h;
@@ -461,8 +473,8 @@ extern "C" int bf_op_load(bf_ctx_t ctx, const char* path, bf_op_t* out) {
       set_error("bf_op_load: %s is truncated or inconsistent", path);
       return BF_EINVAL;
     }
-    const uint64_t nbytes = op.near ? (uint64_t)op.near->a_entries * sizeof(float4) : 0;
-    if (op.near && (op.near->a_entries < 0 || nbytes / sizeof(float4) != (uint64_t)op.near->a_entries)) {
+    const uint64_t nbytes = op.near ? (uint64_t)op.near->a_entries * sizeof(double2) : 0;
+    if (op.near && (op.near->a_entries < 0 || nbytes / sizeof(double2) != (uint64_t)op.near->a_entries)) {
       set_error("bf_op_load: %s is inconsistent (near field size)", path);
       return BF_EINVAL;
     }
@@ -515,12 +527,12 @@ extern "C" int bf_op_load(bf_ctx_t ctx, const char* path, bf_op_t* out) {
         set_error("bf_op_load: %s is inconsistent (near entries)", path);
         return BF_EINVAL;
       }
-      if (cudaMalloc(&op.near->d_A, std::max<uint64_t>(nbytes, 16)) != cudaSuccess) {
+      if (cudaMalloc((void**)&op.near->d_A, std::max<uint64_t>(nbytes, 16)) != cudaSuccess) {
         cudaGetLastError();
         set_error("bf_op_load: cannot allocate the near field");
         return BF_ENOMEM;
       }
-      BF_TRY(get(op.near->d_A, nbytes));
+      BF_TRY(get((void*)op.near->d_A, nbytes));
     }
     uint64_t hh = 0;
     char endm[8];
