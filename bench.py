@@ -890,13 +890,14 @@ def run_ours(args, rank, world, local):
         near_ms = max(ms_full - ms, 1e-6)
         line["near_far"] = {
             "value": world * 1000.0 / ms_full, "unit": UNIT, "ms_per_step": ms_full,
-            "what": "full PetrovGalerkinBF product: near blocks (FP64-evaluated, float-float, "
-                    "self-term r=0 left out) + far butterflies in one device pass",
+            "what": "full PetrovGalerkinBF product: near blocks (complex FP64 entries and FP64 "
+                    "sums, self-term r=0 left out) + far butterflies in one device pass",
             "adjoint": {"value": world * 1000.0 / ms_full_adj, "ms_per_step": ms_full_adj},
             "near_pairs": sn["near_pairs"], "near_entries_both_directions": sn["near_entries"],
             "near_bytes_per_matvec": sn["near_bytes_fwd"],
             "near_ms_per_matvec": near_ms,
             "near_hbm_gbs": sn["near_bytes_fwd"] / (near_ms * 1e-3) / 1e9,
+            "near_fp64_tflops": 8.0 * sn["near_entries"] / 2 / (near_ms * 1e-3) / 1e12,
             "near_setup_seconds": round(near_build_s, 3)}
     if w["storage"] == "ff" and (not args.no_c32 or not args.no_mixed):
         # the same operator with complex FP32 factor storage (half the bytes).  It
