@@ -397,6 +397,13 @@ class Operator:
               "bf_op_add_near")
         return self
 
+    def recompress(self, tau: float) -> "Operator":
+        """``recompress_BF(BF, tau)`` of every far block (``bf_op_recompress``): a new
+        operator with lower ranks; this one is unchanged."""
+        h = C.c_void_p()
+        check(load().bf_op_recompress(self._h, float(tau), C.byref(h)), "bf_op_recompress")
+        return Operator(h.value, self.ctx)
+
     def save(self, path: str):
         """Write the operator to ``path`` (``bf_op_save``): packed layout and factors."""
         check(load().bf_op_save(self._h, os.fsencode(path)), "bf_op_save")

@@ -413,6 +413,21 @@ BF_API int bf_op_mixed_info(bf_op_t op, int64_t* factor_bytes, int64_t* workspac
 BF_API int bf_op_task_shapes(bf_op_t op, int64_t* n_tasks, int32_t* stage, int32_t* kind,
                              int32_t* M, int32_t* n);
 
+/* Butterfly recompression: recompress_BF(BF, tau) of every far block
+ * (src/Butterflyalgebra/algrecomp.jl:19-148): the right pass (R levels from the
+ * last to the second, blocks sharing a column space stacked and compressed by
+ * pivoted QR at rtol tau, the transfer matrix moved into the previous level)
+ * and the left pass (the same on the adjoint).  The stacks of a level are
+ * compressed in one batched launch of the build's pivoted-QR kernel (FP32
+ * Householder, FP64 norms and pivots); Q = A[:, p[1:r]] R11^-1 replaces the
+ * blocks and R[:, invperm(p)] moves into the neighbouring level.  Groups
+ * holding identity blocks are left as they are.  Arithmetic is FP32 (tau
+ * below about 1e-6 gains nothing).  Returns a new operator with the storage
+ * of the input (float-float entries with zero low parts when the input was
+ * float-float); the input is unchanged.  Operators with a near field are
+ * refused (BF_ENOTSUP). */
+BF_API int bf_op_recompress(bf_op_t op, double tau, bf_op_t* out);
+
 /* Persisted operators (no reference counterpart: the reference keeps its
  * factors in memory only and rebuilds them with every assemble_BF,
  * src/ButterflyFactorization/bfassembly.jl:48-200).  bf_op_save writes the

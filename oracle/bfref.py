@@ -657,6 +657,76 @@ def factor_entries(bf: BF) -> int:
 
 
 # --------------------------------------------------------------------------
+# Algebraic recompression (src/Butterflyalgebra/algrecomp.jl)
+# --------------------------------------------------------------------------
+
+
+def pqr(A: np.ndarray, rtol: float):
+    """``LowRankApprox.pqr(A; rtol)`` as called at ``algrecomp.jl:83``: Q (m x r)
+    with orthonormal columns, R (r x n) upper trapezoidal in pivoted column
+    order, and the pivots p, truncated by :func:`pqr_rank`."""
+    Q, R, p = _sp_qr(A, mode="economic", pivoting=True)
+    r = pqr_rank(R, rtol)
+    return Q[:, :r], R[:r, :], p
+
+
+def recompress_right(bf: BF, tau: float, stats: dict | None = None) -> BF:
+    """``recompress_BF_right`` (``algrecomp.jl:45-148``).
+
+    For the R levels from the last to the second (``lold = lr - l + 1``,
+    ``algrecomp.jl:59-61``): the blocks sharing a column key
+    ``(obs_in, src_in)`` are stacked in key order (``:63-78``), the stack is
+    compressed by pivoted QR at rtol ``tau`` (``:83``), its row slices of Q
+    replace the blocks (``:89-101``) and ``T = R[:, invperm(p)]`` (``:86``)
+    multiplies every block of the previous level whose row key
+    ``(obs_out, src_out)`` is that column key (``:115-132``).
+
+    Identity blocks (padding of uneven trees, ``bfassembly.jl:340``) pass one
+    node through unchanged and are alone in their column groups; such a group
+    is left as it is, which is what the pivoted QR of an identity gives
+    (Q = I, T = I).  An identity in the previous level becomes ``T * I = T``.
+    """
+    R = [[Block(b.obs_out, b.src_out, b.obs_in, b.src_in,
+                None if b.data is None else b.data.copy()) for b in lvl] for lvl in bf.R]
+    lr = len(R)
+    for l in range(1, lr):
+        lold = lr - l  # 0-based index of R_factors[lr - l + 1]
+        cur = R[lold]
+        groups: dict = {}
+        for i, b in enumerate(cur):
+            groups.setdefault((b.obs_in, b.src_in), []).append(i)
+        Ru = {}
+        for key in sorted(groups):
+            idx = groups[key]
+            if any(cur[i].data is None for i in idx):
+                continue
+            A = np.vstack([cur[i].data for i in idx])
+            Qm, Rm, p = pqr(A, tau)
+            Ru[key] = Rm[:, np.argsort(p)]
+            row = 0
+            for i in idx:
+                h = cur[i].data.shape[0]
+                cur[i].data = Qm[row:row + h, :].copy()
+                row += h
+            if stats is not None:
+                stats["groups"] = stats.get("groups", 0) + 1
+        for b in R[lold - 1]:
+            T = Ru.get((b.obs_out, b.src_out))
+            if T is not None:
+                b.data = T.copy() if b.data is None else T @ b.data
+    return BF([Block(b.obs_out, b.src_out, b.obs_in, b.src_in, b.data) for b in bf.Q], R,
+              [Block(b.obs_out, b.src_out, b.obs_in, b.src_in, b.data) for b in bf.P],
+              bf.tree_o, bf.tree_s, bf.k, bf.tau, bf.no, bf.ns).wire()
+
+
+def recompress_bf(bf: BF, tau: float, stats: dict | None = None) -> BF:
+    """``recompress_BF`` (``algrecomp.jl:19-31``): the right pass, then the
+    right pass of the adjoint, adjoined back (the left pass)."""
+    right = recompress_right(bf, tau, stats)
+    return adjoint_bf(recompress_right(adjoint_bf(right, "C"), tau, stats), "C")
+
+
+# --------------------------------------------------------------------------
 # Global far-field operator (PetrovGalerkinBF far part)
 # --------------------------------------------------------------------------
 

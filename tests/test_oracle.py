@@ -6,6 +6,7 @@ and adjoints at ``< 1e-2`` (test/test_bfadjtr.jl:133-185); here the same
 criteria run on point-Helmholtz geometries.
 """
 import math
+import os
 
 import numpy as np
 import pytest
@@ -15,6 +16,7 @@ from oracle import bfref as O
 from _util import relerr
 
 TOL = 1e-4
+HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 @pytest.fixture(scope="module")
@@ -154,6 +156,56 @@ def test_global_far_operator_matches_dense():
     assert relerr(y, D @ x) < 10 * TOL
     ya = O.far_matvec(op, x, adjoint=True)
     assert relerr(ya, D.conj().T @ x) < 10 * TOL
+
+
+def test_recompression_meets_reference_criteria(c1):
+    # test/test_algrecomp.jl:72-166: built at 1e-4, recompressed at 1e-2, the
+    # product stays within 10 * 1e-2 of the dense one and the size does not grow
+    n = 4096
+    A = c1["kern"](np.arange(n), np.arange(n))
+    x = G.complex_gaussian(n, 12)
+    st = {}
+    rb = O.recompress_bf(c1["bf"], 1e-2, st)
+    assert st["groups"] > 0
+    assert O.factor_entries(rb) < O.factor_entries(c1["bf"])
+    y = O.matvec_flat(rb, x, np.zeros(n, complex))
+    assert relerr(y, A @ x) < 10 * 1e-2
+    ya = O.matvec_flat(O.adjoint_bf(rb), x, np.zeros(n, complex))
+    assert relerr(ya, A.conj().T @ x) < 10 * 1e-2
+
+
+def test_recompression_right_pass_keeps_orthonormal_stacks(c1):
+    # the last R level's column groups become row slices of one Q (algrecomp.jl:89-97)
+    rb = O.recompress_right(c1["bf"], 1e-3)
+    groups = {}
+    for b in rb.R[-1]:
+        groups.setdefault((b.obs_in, b.src_in), []).append(b.data)
+    for mats in groups.values():
+        Q = np.vstack(mats)
+        assert np.allclose(Q.conj().T @ Q, np.eye(Q.shape[1]), atol=1e-12)
+    # and the product is unchanged up to the truncation
+    x = G.complex_gaussian(4096, 13)
+    y0 = O.matvec_flat(c1["bf"], x, np.zeros(4096, complex))
+    y1 = O.matvec_flat(rb, x, np.zeros(4096, complex))
+    assert relerr(y1, y0) < 10 * 1e-3
+
+
+def test_recompression_with_identity_padding():
+    # uneven trees put identity blocks in the last R level (bfassembly.jl:340);
+    # their groups stay, identities below a compressed group become T
+    from _util import CsrTree, export_to_oracle, oracle_apply
+    g = np.load(os.path.join(HERE, "golden", "plane_unbalanced.npz"))
+    to = CsrTree(g["obs_ptr"], g["obs_idx"])
+    ts = CsrTree(g["src_ptr"], g["src_idx"])
+    bfs = export_to_oracle(g, to, ts)
+    n_ident = sum(b.data is None for bf in bfs for lvl in bf.R for b in lvl)
+    assert n_ident > 0
+    rbs = [O.recompress_bf(bf, 1e-2) for bf in bfs]
+    assert sum(b.data is None for bf in rbs for lvl in bf.R for b in lvl) < n_ident
+    assert sum(map(O.factor_entries, rbs)) < sum(map(O.factor_entries, bfs))
+    n = int(g["n_rows"])
+    assert relerr(oracle_apply(rbs, g["x"], n), g["y"]) < 10 * 1e-2
+    assert relerr(oracle_apply(rbs, g["xa"], int(g["n_cols"]), "C"), g["ya"]) < 10 * 1e-2
 
 
 @pytest.mark.parametrize("name", ["plane_single", "plane_unbalanced", "sphere_far"])
