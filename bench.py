@@ -341,7 +341,9 @@ def run_ncu_case(args, local):
     for _ in range(2):
         op.matvec_ptr(xd.data_ptr(), n, yd.data_ptr(), n, ptr_mode=bfgpu.BF_PTR_DEVICE, stream=sp)
     torch.cuda.synchronize()
-    out = {"ncu_case": args.workload, "levels": op.stats()["n_stages"]}
+    out = {"ncu_case": args.workload, "levels": op.stats()["n_stages"],
+           # algorithmic bytes per level (its launches come after the two matvecs)
+           "stage_bytes": [int(v) for v in op.profile(nrep=1)[1]]}
     if not args.no_mixed:
         op.mixed_info()
         X = np.ascontiguousarray(G.complex_gaussian(n, 12, nrhs=128).T)
@@ -592,6 +594,7 @@ def run_mixed(args, w, stream, world):
 # is moved once), so a level's traffic at another size is this ratio times its
 # algorithmic bytes.  The R ratio is the one of the largest R level.
 TRAFFIC_RATIO = {"plain_c32": {"Q": 0.976, "R": 0.991, "P": 1.002},
+                 "plain_ff": {"Q": 1.001, "R": 1.003, "P": 1.001},
                  "mixed": {"Q": 0.979, "R": 0.981, "P": 0.999}}
 TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum per level launch at 16,384 "
                   "points, as a ratio to the level's algorithmic bytes, times this level's "
