@@ -58,6 +58,8 @@ WORKLOADS = {
 DENSE_ROWS = {"sphere262k": 2048}  # sampled dense rows per workload (default 256)
 BATCH = {"batch32": 32, "batch4": 4}  # operator-batch workloads: number of operators
 SURROGATE = {"surrogate524k": 524288}  # held-out ellipsoid size of the surrogate study
+ROWS = {"rows": "GPU trees and lists (262,144-point sphere), persisted operator (65,536-point "
+                "sphere), recompression of one far block (plane pairs of 16,384 and 65,536 points)"}
 
 
 def parse():
@@ -66,7 +68,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + sorted(BATCH) + sorted(SURROGATE),
+    ap.add_argument("--workload",
+                    choices=sorted(WORKLOADS) + sorted(BATCH) + sorted(SURROGATE) + sorted(ROWS),
                     default="sphere262k")
     ap.add_argument("--storage", choices=["ff", "c32"], default="ff",
                     help="factor storage of the headline operator: float-float (16 B per "
@@ -315,6 +318,123 @@ def run_surrogate(args, rank, world, local):
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def _median_time(fn, reps=3, warmup=1):
+    """Median wall time of fn() over reps calls after warmup calls (fn synchronises)."""
+    for _ in range(warmup):
+        fn()
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        fn()
+        ts.append(time.perf_counter() - t0)
+    return statistics.median(ts)
+
+
+def run_rows(args, rank, world, local):
+    """The widening rows next to the matvec, each timed beside its CPU counterpart:
+    cluster tree + near/far lists (GPU vs the host C++ versions, which restate
+    bisection_tree.jl / intlists.jl), a persisted operator (write and read back), and
+    butterfly recompression of one far block (GPU vs the oracle's restatement of
+    recompress_BF on the same blocks)."""
+    import tempfile as _tf
+    import torch
+    import bfgpu
+    from bfgpu import geometry as G
+    from oracle import bfref as O
+    torch.cuda.set_device(local)
+    if rank != 0:
+        return
+    ctx = bfgpu.Context(local)
+    line = {"metric": "GPU tree + near/far lists, 262,144-point sphere (ms)", "unit": "ms",
+            "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
+            "config": {"workload": ROWS[args.workload]}}
+    # trees and lists (the call a user makes: points in, host arrays out)
+    n = 262144
+    pts = G.fibonacci_sphere(n)
+    t_host = _median_time(lambda: bfgpu.Tree.build(pts, max_points=32))
+    t_gpu = _median_time(lambda: bfgpu.Tree.build_gpu(pts, max_points=32, ctx=ctx))
+    th, tg = bfgpu.Tree.build(pts, max_points=32), bfgpu.Tree.build_gpu(pts, max_points=32, ctx=ctx)
+    same_tree = all(np.array_equal(getattr(th, k), getattr(tg, k)) for k in
+                    ("center", "halfsize", "level", "parent", "first_child", "n_child", "perm",
+                     "begin", "end"))
+
+    def host_lists():
+        far, _ = bfgpu.nearandfar(th, th)
+        return far, bfgpu.near_pairs(th, th)
+    l_host = _median_time(host_lists)
+    l_gpu = _median_time(lambda: bfgpu.nearandfar_gpu(th, th, ctx=ctx))
+    fh, nh = host_lists()
+    fg, ng = bfgpu.nearandfar_gpu(th, th, ctx=ctx)
+    line["value"] = 1e3 * (t_gpu + l_gpu)
+    line["trees_lists"] = {
+        "tree_ms": {"gpu": 1e3 * t_gpu, "host": 1e3 * t_host}, "identical_tree": bool(same_tree),
+        "lists_ms": {"gpu": 1e3 * l_gpu, "host": 1e3 * l_host},
+        "identical_lists": bool(np.array_equal(fh, fg) and np.array_equal(nh, ng)),
+        "far_pairs": int(len(fg)), "near_pairs": int(len(ng)),
+        "host_threads": os.cpu_count(),
+        "what": "host: bf_tree_build + bf_nearandfar + bf_near_pairs (each list call counts, "
+                "then fills); gpu: bf_tree_build_gpu + bf_nearandfar_gpu"}
+    # persisted operator: the 65,536-point sphere's far field, complex FP32 factors
+    n2 = 65536
+    p2 = G.fibonacci_sphere(n2)
+    t2 = bfgpu.Tree.build(p2, max_points=32)
+    op = bfgpu.PetrovGalerkinBF(p2, p2, t2, t2, G.wavenumber(n2, 4 * math.pi), tol=1e-4, ctx=ctx)
+    x = G.complex_gaussian(n2, 3)
+    y0 = op.matvec(x)
+    with _tf.TemporaryDirectory() as d:
+        path = os.path.join(d, "sphere65k.bfop")
+        t0 = time.perf_counter()
+        op.save(path)
+        t_save = time.perf_counter() - t0
+        size = os.path.getsize(path)
+        t0 = time.perf_counter()
+        back = bfgpu.load_operator(path, ctx)
+        t_load = time.perf_counter() - t0
+        same = bool(np.array_equal(back.matvec(x), y0))
+        del back
+    line["persisted"] = {"operator": "sphere65k far field, complex FP32 factors",
+                         "file_bytes": int(size), "save_s": t_save, "load_s": t_load,
+                         "save_gbs": size / t_save / 1e9, "load_gbs": size / t_load / 1e9,
+                         "bit_identical_matvec": same,
+                         "load_checks": "chunk hashes, every offset and length, pair alignment"}
+    del op
+    # recompression of one far block (two parallel unit squares 4 apart)
+    rec = {}
+    for npl, depth, lam, with_cpu in ((16384, 5, 0.0625, True), (65536, 6, 0.03125, False)):
+        obs, src = G.plane_pair(npl, seed=1)
+        to, ts = bfgpu.Tree.build(obs, max_depth=depth), bfgpu.Tree.build(src, max_depth=depth)
+        op = bfgpu.assemble_BF(obs, src, to, ts, 0, 0, 2 * math.pi / lam, 1e-4, c_tau=4.0,
+                               seed=3, ctx=ctx)
+        e0 = op.stats()["factor_entries"]
+        r = {"points": npl, "quadtree_depth": depth, "wavelength": lam, "tol_build": 1e-4,
+             "tau": 1e-2, "r_levels": int(op.stats()["n_stages"]) - 2}
+        holder = {}
+
+        def gpu_rc():
+            holder["op"] = op.recompress(1e-2)
+            torch.cuda.synchronize()
+        r["gpu_s"] = _median_time(gpu_rc)
+        rop = holder["op"]
+        xs = G.complex_gaussian(npl, 4)
+        ya = op.matvec(xs)
+        r["factor_entries"] = {"built": int(e0), "recompressed": int(rop.stats()["factor_entries"])}
+        r["rel_diff_vs_built"] = float(np.linalg.norm(rop.matvec(xs) - ya) / np.linalg.norm(ya))
+        if with_cpu:
+            bfs = O.from_blocks(op.export_blocks(), O.CsrTree(*to.values_csr()),
+                                O.CsrTree(*ts.values_csr()))
+            t0 = time.perf_counter()
+            rbs = [O.recompress_bf(bf, 1e-2) for bf in bfs]
+            r["oracle_cpu_s"] = time.perf_counter() - t0
+            r["oracle_cpu_threads"] = 1
+            r["factor_entries"]["oracle"] = int(sum(O.factor_entries(b) for b in rbs))
+            yo = O.apply_far(rbs, xs, npl)
+            r["rel_diff_vs_oracle"] = float(np.linalg.norm(rop.matvec(xs) - yo) / np.linalg.norm(yo))
+        rec[f"plane{npl // 1024}k"] = r
+        del op, rop
+    line["recompression"] = rec
+    print(json.dumps(line), flush=True)
 
 
 def run_ncu_case(args, local):
@@ -943,6 +1063,13 @@ def main():
         run_ncu_case(args, local)
     elif args.workload in BATCH and args.impl != "reference":
         run_batch(args, rank, world, local)
+    elif args.workload in ROWS:
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable":
+                              "the reference's trees, lists and recompression are Julia; the "
+                              "rows line times their CPU restatements beside the GPU"}))
+        else:
+            run_rows(args, rank, world, local)
     elif args.workload in SURROGATE:
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable":

@@ -657,6 +657,63 @@ def factor_entries(bf: BF) -> int:
 
 
 # --------------------------------------------------------------------------
+# Exchange with the C-ABI block layout (bf_op_export_blocks / bf_factor_desc)
+# --------------------------------------------------------------------------
+
+
+class CsrTree:
+    """The part of the tree contract the matvecs use (``values(node)``), from a
+    node -> values CSR map (ptr, idx)."""
+
+    def __init__(self, ptr, idx):
+        self.ptr = np.asarray(ptr, np.int64)
+        self.idx = np.asarray(idx, np.int64)
+
+    def values(self, node):
+        return self.idx[self.ptr[node]:self.ptr[node + 1]]
+
+
+def from_blocks(ex, tree_o, tree_s, k: float = 0.0, tau: float = 0.0) -> list:
+    """Exported block arrays (keys, stage, shapes, identity flags, column-major data)
+    -> one pointer-wired BF per far block; stage 0 = Q, -1 = P, l = R level l."""
+    nbf = int(ex["bf"].max()) + 1 if len(ex["bf"]) else 0
+    per = [dict(Q=[], R={}, P=[]) for _ in range(nbf)]
+    for b in range(len(ex["bf"])):
+        f, st = int(ex["bf"][b]), int(ex["stage"][b])
+        if ex["identity"][b]:
+            data = None
+        else:
+            r, c, off = int(ex["rows"][b]), int(ex["cols"][b]), int(ex["data_off"][b])
+            data = ex["data"][off:off + r * c].reshape((r, c), order="F")
+        blk = Block(int(ex["obs_out"][b]), int(ex["src_out"][b]), int(ex["obs_in"][b]),
+                    int(ex["src_in"][b]), data)
+        if st == 0:
+            per[f]["Q"].append(blk)
+        elif st < 0:
+            per[f]["P"].append(blk)
+        else:
+            per[f]["R"].setdefault(st, []).append(blk)
+    out = []
+    for f in range(nbf):
+        d = per[f]
+        R = [d["R"][lv] for lv in sorted(d["R"])]
+        no = d["Q"][0].obs_out if d["Q"] else 0
+        ns = d["P"][0].src_out if d["P"] else 0
+        out.append(BF(d["Q"], R, d["P"], tree_o, tree_s, k, tau, no, ns).wire())
+    return out
+
+
+def apply_far(bfs: list, x: np.ndarray, n_out: int, op: str = "N") -> np.ndarray:
+    """op(A) x over a list of BFs: the reference-order flat matvec of each, through
+    the materialised adjoint / transpose for "C" / "T"."""
+    y = np.zeros(n_out, np.complex128)
+    for bf in bfs:
+        b = bf if op == "N" else adjoint_bf(bf, op)
+        matvec_flat(b, x, y, 1.0, 1.0)
+    return y
+
+
+# --------------------------------------------------------------------------
 # Algebraic recompression (src/Butterflyalgebra/algrecomp.jl)
 # --------------------------------------------------------------------------
 

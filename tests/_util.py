@@ -68,51 +68,17 @@ def relerr(a, b):
 def export_to_oracle(ex, tree_o, tree_s, k=0.0, tau=0.0):
     """bf_op_export_blocks arrays -> list of oracle BF objects (pointer-wired)."""
     from oracle import bfref as O
-    nbf = int(ex["bf"].max()) + 1 if len(ex["bf"]) else 0
-    per = [dict(Q=[], R={}, P=[]) for _ in range(nbf)]
-    for b in range(len(ex["bf"])):
-        f, st = int(ex["bf"][b]), int(ex["stage"][b])
-        if ex["identity"][b]:
-            data = None
-        else:
-            r, c, off = int(ex["rows"][b]), int(ex["cols"][b]), int(ex["data_off"][b])
-            data = ex["data"][off:off + r * c].reshape((r, c), order="F")
-        blk = O.Block(int(ex["obs_out"][b]), int(ex["src_out"][b]), int(ex["obs_in"][b]),
-                      int(ex["src_in"][b]), data)
-        if st == 0:
-            per[f]["Q"].append(blk)
-        elif st < 0:
-            per[f]["P"].append(blk)
-        else:
-            per[f]["R"].setdefault(st, []).append(blk)
-    out = []
-    for f in range(nbf):
-        d = per[f]
-        R = [d["R"][l] for l in sorted(d["R"])]
-        no = d["Q"][0].obs_out if d["Q"] else 0
-        ns = d["P"][0].src_out if d["P"] else 0
-        out.append(O.BF(d["Q"], R, d["P"], tree_o, tree_s, k, tau, no, ns).wire())
-    return out
+    return O.from_blocks(ex, tree_o, tree_s, k, tau)
 
 
-class CsrTree:
-    """The part of the tree contract the oracle matvec uses (``values(node)``),
-    from a node -> values CSR map (ptr, idx)."""
-
-    def __init__(self, ptr, idx):
-        self.ptr = np.asarray(ptr, np.int64)
-        self.idx = np.asarray(idx, np.int64)
-
-    def values(self, node):
-        return self.idx[self.ptr[node]:self.ptr[node + 1]]
+def CsrTree(ptr, idx):
+    """node -> values CSR map as an oracle tree (``values(node)``)."""
+    from oracle import bfref as O
+    return O.CsrTree(ptr, idx)
 
 
 def oracle_apply(bfs, x, n_out, op="N"):
     """Oracle far-field product op(A) x over the BF list (reference-order flat
     matvec of each block, the materialised adjoint / transpose for "C" / "T")."""
     from oracle import bfref as O
-    y = np.zeros(n_out, np.complex128)
-    for bf in bfs:
-        b = bf if op == "N" else O.adjoint_bf(bf, op)
-        O.matvec_flat(b, x, y, 1.0, 1.0)
-    return y
+    return O.apply_far(bfs, x, n_out, op)
