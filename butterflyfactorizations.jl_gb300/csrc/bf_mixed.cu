@@ -23,7 +23,7 @@
 //     stored blocks as MN-major B operands (Ahat^T is the real form of A^H);
 //     the transpose conjugates inputs and outputs on top of that.
 //
-// Pipeline per CTA (4 warps, 4 CTAs per SM, 128 tensor-memory columns each):
+// Pipeline per CTA (4 warps, 8 CTAs per SM, 64 tensor-memory columns each):
 // two stages of shared memory, each one input chunk (8 entries x 128
 // right-hand sides, hi and lo) plus the matching factor blocks.  Thread 0
 // issues the bulk copies of the factor blocks and the MMAs; all 128 threads
@@ -49,12 +49,13 @@ constexpr int MX_R = 128;                         // right-hand sides per chunk 
 constexpr int MX_THREADS = 128;
 constexpr int MX_IB = 1;                          // input blocks (of 8 entries) per stage
 constexpr int MX_IC = MX_IB * 8;                  // input entries per stage
-constexpr int MX_OB = 8;                          // output blocks per unit (N <= 128)
-constexpr int MX_TCOLS = 128;                     // tensor-memory columns per CTA
-constexpr int MX_CTAS_PER_SM = 4;                 // 4 x 32 KB shared memory, 4 x 128 TMEM columns
+constexpr int MX_OB = 4;                          // output blocks per unit (N <= 64)
+constexpr int MX_TCOLS = 64;                      // tensor-memory columns per CTA
+constexpr int MX_CTAS_PER_SM = 8;                 // 8 x 24 KB shared memory, 8 x 64 TMEM columns,
+                                                  // 8 x 128 threads x 64 registers
 constexpr int MX_XPLANE = (MX_IC / 4) * 2048;     // one BF16 plane of the input tile (8 KB)
 constexpr int MX_XBYTES = 2 * MX_XPLANE;          // hi + lo
-constexpr int MX_FBYTES = MX_OB * MX_IB * 1024;   // factor blocks of one stage (16 KB)
+constexpr int MX_FBYTES = MX_OB * MX_IB * 1024;   // factor blocks of one stage (4 KB)
 constexpr int MX_STAGE = MX_XBYTES + MX_FBYTES;
 constexpr int MX_NST = 2;
 constexpr size_t MX_SMEM = (size_t)MX_NST * MX_STAGE + 256;
