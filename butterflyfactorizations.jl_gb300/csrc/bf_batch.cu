@@ -356,10 +356,10 @@ struct bf_batch {
 
 using namespace bfg;
 
-extern "C" {
+namespace bfg {
 
-int bf_batch_create_op(bf_ctx_t ctx, bf_op_t const* ops, const int32_t* trans,
-                       const int32_t* nrhs, int32_t n_ops, int32_t rhs_chunk, bf_batch_t* out) {
+int batch_create(Context* ctx, Operator* const* ops, const int32_t* trans, const int32_t* nrhs,
+                 int32_t n_ops, int32_t rhs_chunk, bf_batch** out) {
   try {
     if (!ctx || !ops || !nrhs || n_ops <= 0 || !out) {
       set_error("bf_batch_create: invalid arguments");
@@ -368,7 +368,7 @@ int bf_batch_create_op(bf_ctx_t ctx, bf_op_t const* ops, const int32_t* trans,
     if (rhs_chunk <= 0) rhs_chunk = 8;
     auto h = std::make_unique<bf_batch>();
     BatchState& b = h->s;
-    b.ctx = &ctx->c;
+    b.ctx = ctx;
     b.rhs_chunk = rhs_chunk;
     int maxr = 0;
     for (int i = 0; i < n_ops; ++i) {
@@ -381,7 +381,7 @@ int bf_batch_create_op(bf_ctx_t ctx, bf_op_t const* ops, const int32_t* trans,
         set_error("bf_batch_create: operator %d has invalid trans %d", i, tr);
         return BF_EINVAL;
       }
-      Operator& op = ops[i]->op;
+      Operator& op = *ops[i];
       if (op.near) {
         set_error("bf_batch_create: operator %d has a near field; batches apply far fields "
                   "(use bf_matvec for near + far)", i);
@@ -471,6 +471,38 @@ int bf_batch_create_op(bf_ctx_t ctx, bf_op_t const* ops, const int32_t* trans,
     set_error("bf_batch_create: %s", e.what());
     return BF_ENOMEM;
   }
+}
+
+void batch_destroy(bf_batch* b) { delete b; }
+
+int batch_buffers(bf_batch* b, int op, double2** x, double2** y) {
+  if (!b || op < 0 || op >= (int)b->s.hops.size()) {
+    set_error("batch: invalid operator index");
+    return BF_EINVAL;
+  }
+  *x = (double2*)b->s.hops[op].X;
+  *y = b->s.hops[op].Y;
+  return BF_OK;
+}
+
+int batch_launch(bf_batch* b, cudaStream_t st) {
+  BF_TRY_CUDA(cudaGraphLaunch(b->s.exec, st));
+  return BF_OK;
+}
+
+}  // namespace bfg
+
+extern "C" {
+
+int bf_batch_create_op(bf_ctx_t ctx, bf_op_t const* ops, const int32_t* trans,
+                       const int32_t* nrhs, int32_t n_ops, int32_t rhs_chunk, bf_batch_t* out) {
+  if (!ctx || !ops || !nrhs || n_ops <= 0 || !out) {
+    set_error("bf_batch_create: invalid arguments");
+    return BF_EINVAL;
+  }
+  std::vector<Operator*> v((size_t)n_ops);
+  for (int i = 0; i < n_ops; ++i) v[i] = ops[i] ? &ops[i]->op : nullptr;
+  return batch_create(&ctx->c, v.data(), trans, nrhs, n_ops, rhs_chunk, out);
 }
 
 int bf_batch_create(bf_ctx_t ctx, bf_op_t const* ops, const int32_t* nrhs, int32_t n_ops,

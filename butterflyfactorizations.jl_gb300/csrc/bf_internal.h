@@ -344,6 +344,19 @@ struct Context {
   cudaDeviceProp prop{};
 };
 
+}  // namespace bfg
+struct bf_batch;  // bf_batch.cu
+namespace bfg {
+
+// Operator batches (bf_batch.cu), also used by bf_matvec for chunks of
+// MRHS_CHUNK right-hand sides of one operator
+constexpr int MRHS_CHUNK = 8;
+int batch_create(Context* ctx, struct Operator* const* ops, const int32_t* trans,
+                 const int32_t* nrhs, int32_t n_ops, int32_t rhs_chunk, bf_batch** out);
+void batch_destroy(bf_batch* b);
+int batch_buffers(bf_batch* b, int op, double2** x, double2** y);
+int batch_launch(bf_batch* b, cudaStream_t st);
+
 struct Operator {
   Context* ctx = nullptr;
   cudaStream_t stream = nullptr;
@@ -372,6 +385,11 @@ struct Operator {
   int* h_err_dev = nullptr;    // device address of h_err
   long long wait_limit = -1;   // polls of a bounded wait; < 0: the default (about 1 s)
   int store_ff = 0;            // GPU-built factors widened to float-float (16 B) storage
+  // one-operator batches of MRHS_CHUNK columns per direction (N, C, T), made at
+  // the first bf_matvec call with that many right-hand sides; 1 in mrhs_off:
+  // the batch could not be made (its memory), columns run one by one
+  bf_batch* mrhs[3] = {nullptr, nullptr, nullptr};
+  int mrhs_off[3] = {0, 0, 0};
   // staging of host right-hand sides
   double* d_x = nullptr;
   double* d_y = nullptr;

@@ -227,6 +227,8 @@ inline int grid_for(int64_t n, int threads) {
 }  // namespace
 
 Operator::~Operator() {
+  for (bf_batch*& b : mrhs)
+    if (b) batch_destroy(b);
   if (mixed) mixed_free(mixed);
   if (near) near_free(near);
   if (d_raw) cudaFree(d_raw);
@@ -450,6 +452,70 @@ static int matvec_one(Operator& op, int trans, const double2* x, double2* y, dou
   return BF_OK;
 }
 
+// y[:, c] = alpha * z[:, c] + beta * y[:, c] (beta == 0: y is not read); z packed n x ncol
+__global__ void axpby_kernel(double2* __restrict__ y, int64_t ldy, const double2* __restrict__ z,
+                             int64_t n, int ncol, double2 a, double2 b, int bzero) {
+  const int64_t tot = n * ncol;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = e / n, i = e - c * n;
+    const double2 v = z[e];
+    double2 r = make_double2(a.x * v.x - a.y * v.y, a.x * v.y + a.y * v.x);
+    if (!bzero) {
+      const double2 w = y[c * ldy + i];
+      r.x += b.x * w.x - b.y * w.y;
+      r.y += b.x * w.y + b.y * w.x;
+    }
+    y[c * ldy + i] = r;
+  }
+}
+
+// The columns of one call (device pointers).  Forward: whole chunks of
+// MRHS_CHUNK go through the operator's own one-operator batch, where each
+// factor entry loaded serves up to four right-hand sides (the reference's
+// bfmatrix.jl:10-75 applies the operator column by column); measured at
+// 262,144 points with 32 columns: 1.43x (float-float factors) and 1.10x
+// (complex FP32) over the column loop.  The batch's adjoint was not faster
+// (1.07x, 0.89x), so adjoint and transpose columns, the remainder columns and
+// every column of an operator with a near field go one by one.
+static int matvec_cols(Operator& op, int trans, int64_t nrhs, const double2* x, int64_t ldx,
+                       double2* y, int64_t ldy, double2 a, double2 b, cudaStream_t st) {
+  const Plan& p = op.plan;
+  const int64_t nin = trans == BF_OP_N ? p.n_cols : p.n_rows;
+  const int64_t nout = trans == BF_OP_N ? p.n_rows : p.n_cols;
+  const int ti = trans == BF_OP_N ? 0 : trans == BF_OP_C ? 1 : 2;
+  const int bzero = b.x == 0.0 && b.y == 0.0;
+  int64_t c = 0;
+  if (trans == BF_OP_N && nrhs >= MRHS_CHUNK && !op.near && !op.mrhs_off[ti]) {
+    if (!op.mrhs[ti]) {
+      Operator* self = &op;
+      const int32_t tr = trans, nr = MRHS_CHUNK;
+      const int rc = batch_create(op.ctx, &self, &tr, &nr, 1, MRHS_CHUNK, &op.mrhs[ti]);
+      if (rc == BF_ENOMEM) {  // not enough device memory for the batch: columns one by one
+        op.mrhs_off[ti] = 1;
+        op.mrhs[ti] = nullptr;
+      } else {
+        BF_TRY(rc);
+      }
+    }
+    if (op.mrhs[ti]) {
+      double2 *bx = nullptr, *by = nullptr;
+      BF_TRY(batch_buffers(op.mrhs[ti], 0, &bx, &by));
+      for (; c + MRHS_CHUNK <= nrhs; c += MRHS_CHUNK) {
+        BF_TRY_CUDA(cudaMemcpy2DAsync(bx, nin * sizeof(double2), x + c * ldx, ldx * sizeof(double2),
+                                      nin * sizeof(double2), MRHS_CHUNK, cudaMemcpyDeviceToDevice,
+                                      st));
+        BF_TRY(batch_launch(op.mrhs[ti], st));
+        axpby_kernel<<<grid_for(nout * MRHS_CHUNK, 256), 256, 0, st>>>(y + c * ldy, ldy, by, nout,
+                                                                       MRHS_CHUNK, a, b, bzero);
+        BF_TRY_CUDA(cudaGetLastError());
+      }
+    }
+  }
+  for (; c < nrhs; ++c) BF_TRY(matvec_one(op, trans, x + c * ldx, y + c * ldy, a, b, st, op.d_ws));
+  return BF_OK;
+}
+
 int take_device_error(Operator& op, const char* what) {
   if (!op.h_err) return BF_OK;
   const int e = __atomic_exchange_n(op.h_err, 0, __ATOMIC_ACQ_REL);
@@ -530,12 +596,8 @@ int run_matvec(Operator& op, int trans, int64_t nrhs, const double* x, int64_t l
   const bool bzero = b.x == 0.0 && b.y == 0.0;
   BF_TRY_CUDA(cudaSetDevice(op.ctx->device));
   cudaStream_t st = stream ? stream : op.stream;
-  if (ptr_mode == BF_PTR_DEVICE) {
-    for (int64_t c = 0; c < nrhs; ++c)
-      BF_TRY(matvec_one(op, trans, (const double2*)(x + 2 * c * ldx), (double2*)(y + 2 * c * ldy),
-                        a, b, st, op.d_ws));
-    return BF_OK;
-  }
+  if (ptr_mode == BF_PTR_DEVICE)
+    return matvec_cols(op, trans, nrhs, (const double2*)x, ldx, (double2*)y, ldy, a, b, st);
   if (ptr_mode != BF_PTR_HOST) {
     set_error("bf_matvec: invalid ptr_mode %d", ptr_mode);
     return BF_EINVAL;
@@ -556,9 +618,8 @@ int run_matvec(Operator& op, int trans, int64_t nrhs, const double* x, int64_t l
   if (!bzero)
     BF_TRY_CUDA(cudaMemcpy2DAsync(op.d_y, nout * 2 * sizeof(double), y, ldy * 2 * sizeof(double),
                                   nout * 2 * sizeof(double), nrhs, cudaMemcpyHostToDevice, st));
-  for (int64_t c = 0; c < nrhs; ++c)
-    BF_TRY(matvec_one(op, trans, (const double2*)(op.d_x + 2 * c * nin),
-                      (double2*)(op.d_y + 2 * c * nout), a, b, st, op.d_ws));
+  BF_TRY(matvec_cols(op, trans, nrhs, (const double2*)op.d_x, nin, (double2*)op.d_y, nout, a, b,
+                     st));
   BF_TRY_CUDA(cudaMemcpy2DAsync(y, ldy * 2 * sizeof(double), op.d_y, nout * 2 * sizeof(double),
                                 nout * 2 * sizeof(double), nrhs, cudaMemcpyDeviceToHost, st));
   BF_TRY_CUDA(cudaStreamSynchronize(st));

@@ -282,6 +282,11 @@ BF_API int bf_import_factors(bf_ctx_t ctx, const bf_factor_desc* desc, bf_op_t* 
  * forward factors (no copy; cf. src/Butterflyalgebra/bfadjtr.jl:43-67).
  * x, y: complex (re,im) doubles; alpha, beta: complex scalars as double[2].
  * stream: a cudaStream_t, or NULL for the handle's own stream.
+ * Forward calls with nrhs >= 8 on an operator without a near field run whole
+ * chunks of 8 columns through a one-operator batch (each factor entry loaded
+ * serves up to 4 columns); its buffers (8 workspaces, 8 columns of x and y)
+ * are allocated at the first such call and kept with the handle.  If they do
+ * not fit, the columns run one by one.
  * ------------------------------------------------------------------------ */
 BF_API int bf_matvec(bf_op_t op, int trans, int64_t nrhs, const double* x, int64_t ldx,
                      double* y, int64_t ldy, const double* alpha, const double* beta,

@@ -56,6 +56,37 @@ def test_alpha_beta_and_multi_rhs(c1):
         assert relerr(Y[:, j], ref) <= PARITY
 
 
+@pytest.mark.parametrize("d", ["N", "C", "T"])
+def test_many_rhs_chunks(c1, d):
+    """19 right-hand sides: forward, two chunks of 8 through the operator's one-operator
+    batch and three columns one by one (adjoint and transpose: column by column);
+    alpha/beta, host and device pointers."""
+    torch = pytest.importorskip("torch")
+    op = {"N": c1["op"], "C": c1["op"].adjoint(), "T": c1["op"].transpose()}[d]
+    bf = c1["bf"] if d == "N" else O.adjoint_bf(c1["bf"], d)
+    X = G.complex_gaussian(4096, 26, nrhs=19)
+    Y0 = G.complex_gaussian(4096, 27, nrhs=19)
+    alpha, beta = 0.75 + 1j, -0.5 + 0.125j
+    refs = [O.matvec_flat(bf, X[:, j], Y0[:, j].copy(), alpha, beta) for j in range(19)]
+    Y = Y0.copy(order="F")
+    bfgpu.mul(Y, op, X, alpha, beta)
+    for j in range(19):
+        assert relerr(Y[:, j], refs[j]) <= PARITY, j
+    # device pointers with leading dimensions above the sizes; beta = 0 reads no y
+    ld = 4100
+    xd = torch.zeros((19, ld), dtype=torch.complex128, device="cuda")
+    xd[:, :4096] = torch.from_numpy(np.ascontiguousarray(X.T)).cuda()
+    yd = torch.full((19, ld), float("nan"), dtype=torch.complex128, device="cuda")
+    torch.cuda.synchronize()
+    op.matvec_device(xd.data_ptr(), ld, yd.data_ptr(), ld, nrhs=19, alpha=alpha)
+    torch.cuda.synchronize()
+    Yd = yd[:, :4096].cpu().numpy().T
+    for j in range(19):
+        ref = O.matvec_flat(bf, X[:, j], np.zeros(4096, complex), alpha, 0.0)
+        assert relerr(Yd[:, j], ref) <= PARITY, j
+    assert torch.isnan(yd[:, 4096:]).all()  # nothing past each column's end is written
+
+
 def test_device_pointers(c1):
     torch = pytest.importorskip("torch")
     x = G.complex_gaussian(4096, 25)
