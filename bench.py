@@ -905,6 +905,7 @@ def run_ours(args, rank, world, local):
     import gc
     import torch
     import bfgpu
+    from bfgpu import geometry as G
     torch.cuda.set_device(local)
     w = build_workload(args.workload, local, args.storage)
     op = w["op"]
@@ -962,6 +963,27 @@ def run_ours(args, rank, world, local):
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_s = max_over_ranks(e2e_s, world)
 
+    # 32 right-hand sides in one bf_matvec call (forward chunks of 8 through the
+    # handle's one-operator batch), CUDA events around the call
+    NR = 32
+    xm = torch.from_numpy(np.ascontiguousarray(G.complex_gaussian(n, 41, nrhs=NR).T)).cuda()
+    ym = torch.zeros_like(xm)
+
+    def step_multi():
+        op.matvec_ptr(xm.data_ptr(), n, ym.data_ptr(), n, nrhs=NR,
+                      ptr_mode=bfgpu.BF_PTR_DEVICE, stream=sp)
+    for _ in range(2):
+        step_multi()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(max(2, args.steps // 8)):
+        step_multi()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    op.check(sp)
+    ms_multi = e0.elapsed_time(e1) / max(2, args.steps // 8)
+    del xm, ym
+
     # roofline of the dominant level launch (CUDA events inside the library)
     adj_stage_ms, _, _ = opa.profile(nrep=3)
     roof, kernels = plain_roofline(op, w["storage"])
@@ -986,6 +1008,10 @@ def run_ours(args, rank, world, local):
                     "hbm_gbs": st["alg_bytes_fwd"] / (ms_adj * 1e-3) / 1e9},
         "e2e": {"value": world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 16 * n,
                 "d2h_bytes_per_step": 16 * n},
+        "multi_rhs": {"value": world * NR * 1000.0 / ms_multi, "unit": UNIT, "rhs_per_call": NR,
+                      "ms_per_call": ms_multi, "over_single": ms * NR / ms_multi,
+                      "what": "one FP64 bf_matvec call with 32 columns: chunks of 8 through "
+                              "the handle's one-operator batch"},
         "roofline": roof,
         "gpu_launches": int(kernels * args.steps),
         "clocks": clocks,
