@@ -12,7 +12,7 @@ using LinearAlgebra
 using LinearMaps
 using ButterflyFactorizations: cluster_root, cluster_children, cluster_values, cluster_center,
                                cluster_radius, cluster_testtree, cluster_trialtree
-import ButterflyFactorizations: PetrovGalerkinBF, assemble_BF
+import ButterflyFactorizations: PetrovGalerkinBF, assemble_BF, recompress_BF
 
 const lib = get(ENV, "BFGPU_LIB", joinpath(@__DIR__, "..", "bfgpu", "libbfgpu.so"))
 
@@ -252,27 +252,87 @@ function _build(ctx::Context, X::AbstractMatrix{Float64}, Y::AbstractMatrix{Floa
 end
 
 """
+    near_pairs_gpu(testtree, trialtree; alpha, minbflvl, leafcomp, leafimbalance)
+
+Near pairs (library node ids, 0-based) of the same traversal as nearandfar_gpu.
+"""
+function near_pairs_gpu(to::GPUTree, ts::GPUTree; alpha=1.0, minbflvl=3, leafcomp=true,
+                        leafimbalance=true)
+    nn = Ref{Int64}(0)
+    args(no, ns, cap) = ccall((:bf_near_pairs, lib), Cint,
+                              (Ptr{Cvoid}, Ptr{Cvoid}, Float64, Int32, Int32, Int32, Ptr{Int64},
+                               Ptr{Int64}, Int64, Ref{Int64}),
+                              to.h, ts.h, alpha, minbflvl, leafcomp, leafimbalance, no, ns, cap,
+                              nn)
+    check(args(C_NULL, C_NULL, 0), "bf_near_pairs")
+    no = zeros(Int64, max(nn[], 1)); ns = zeros(Int64, max(nn[], 1))
+    check(args(no, ns, length(no)), "bf_near_pairs")
+    return no[1:nn[]], ns[1:nn[]]
+end
+
+"""
     PetrovGalerkinBF(HelmholtzPoints(), X, Y, tree, k; tol=1e-3, alpha=1.0, Ctau=2.9592,
                      minbflvl=3, leafcomp=true, leafimbalance=true, adaptive=true,
-                     farfieldonly=true, storage=:c32, ctx=Context(0))
+                     farfieldonly=false, storage=:c32, ctx=Context(0))
 
-The far field of the reference's PetrovGalerkinBF (petrovgalerkinbf.jl:33-54)
-built on the GPU: the trees of `tree` (cluster_testtree / cluster_trialtree)
-are converted, the far pairs come from nearandfar_gpu, and every far pair is
-compressed by bf_build.  Returns a GPUButterflyOperator (a LinearMap).
-`storage = :ff` keeps the factors as 16-byte float-float entries.
+The reference's PetrovGalerkinBF (petrovgalerkinbf.jl:33-54) built on the GPU:
+the trees of `tree` (cluster_testtree / cluster_trialtree) are converted, the
+far pairs come from nearandfar_gpu and every far pair is compressed by
+bf_build; unless `farfieldonly` (the reference's default is false) the near
+blocks of the near pairs are evaluated on the GPU and attached
+(bf_op_add_near), so that mul! gives near + far as in matrixvector.jl:28-33.
+Returns a GPUButterflyOperator (a LinearMap).  `storage = :ff` keeps the far
+factors as 16-byte float-float entries.
 """
 function PetrovGalerkinBF(::HelmholtzPoints, X::AbstractMatrix{Float64},
                           Y::AbstractMatrix{Float64}, tree, k::Float64; tol=1e-3, alpha=1.0,
                           Ctau=2.9592, minbflvl=3, leafcomp=true, leafimbalance=true,
-                          adaptive=true, farfieldonly=true, seed=0, min_samples=10,
+                          adaptive=true, farfieldonly=false, seed=0, min_samples=10,
                           storage=:c32, ctx::Context=Context(0))
-    farfieldonly || error("the GPU operator holds the far field only")
     to = GPUTree(cluster_testtree(tree), size(X, 2))
     ts = GPUTree(cluster_trialtree(tree), size(Y, 2))
     fo, fs, _ = nearandfar_gpu(to, ts; alpha, minbflvl, leafcomp, leafimbalance)
-    return _build(ctx, X, Y, to, ts, fo, fs, k, tol; c_tau=Ctau, adaptive=Int32(adaptive),
-                  seed=UInt64(seed), min_samples=Int32(min_samples), storage)
+    A = _build(ctx, X, Y, to, ts, fo, fs, k, tol; c_tau=Ctau, adaptive=Int32(adaptive),
+               seed=UInt64(seed), min_samples=Int32(min_samples), storage)
+    if !farfieldonly
+        no, ns = near_pairs_gpu(to, ts; alpha, minbflvl, leafcomp, leafimbalance)
+        x = Matrix{Float64}(X); y = Matrix{Float64}(Y)
+        check(ccall((:bf_op_add_near, lib), Cint,
+                    (Ptr{Cvoid}, Ptr{Float64}, Int64, Ptr{Float64}, Int64, Ptr{Cvoid},
+                     Ptr{Cvoid}, Ptr{Int64}, Ptr{Int64}, Int64, Float64),
+                    A.h, x, size(x, 2), y, size(y, 2), to.h, ts.h, no, ns, length(no), k),
+              "bf_op_add_near")
+    end
+    return A
+end
+
+"""
+    recompress_BF(A::GPUButterflyOperator, tau)
+
+The reference's recompress_BF (src/Butterflyalgebra/algrecomp.jl:19-31) over
+every far block of A, on the GPU (bf_op_recompress): a new operator, A is
+unchanged.  A must hold the far field only.
+"""
+function recompress_BF(A::GPUButterflyOperator, tau::Real)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:bf_op_recompress, lib), Cint, (Ptr{Cvoid}, Float64, Ref{Ptr{Cvoid}}),
+                A.h, Float64(tau), h), "bf_op_recompress")
+    return _wrap(h[])
+end
+
+"""
+    save(A::GPUButterflyOperator, path) / load(ctx, path)
+
+A built operator to a file and back (bf_op_save / bf_op_load): a second run
+skips the construction.
+"""
+save(A::GPUButterflyOperator, path::AbstractString) =
+    check(ccall((:bf_op_save, lib), Cint, (Ptr{Cvoid}, Cstring), A.h, path), "bf_op_save")
+function load(ctx::Context, path::AbstractString)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:bf_op_load, lib), Cint, (Ptr{Cvoid}, Cstring, Ref{Ptr{Cvoid}}), ctx.h, path, h),
+          "bf_op_load")
+    return _wrap(h[])
 end
 
 """
