@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(256) adj_tall_kernel(const int32_t* __restrict
   const int rg = lane % RG, cg = lane / RG;
   const int32_t* __restrict__ rmap = maps + t.rmap_off;
   const int32_t* __restrict__ cmap = maps + t.cmap_off;
-  const int cpl = min(ADJ_CPL, (t.n + CG - 1) / CG);
+  const int cpl = adj_cpl(t.n, CG);
   const int per_pass = CG * cpl;
   // row split in multiples of RG so that row groups stay aligned
   const int rows_per_warp = ((t.M + 8 * RG - 1) / (8 * RG)) * RG;

@@ -122,13 +122,23 @@ __device__ __forceinline__ void write_out(const DTask& t, const int32_t* __restr
     ws[(long long)cmap[c] * S] = cdf_norm(v);
 }
 
+// Columns per lane and pass for a task of n columns over CG column groups:
+// the fewest passes of at most ADJ_CPL columns per lane, with the columns
+// spread evenly over them.  (Filling every pass but the last would leave most
+// lanes of the last pass idle while it walks all rows again: n = 18 over 4
+// groups is 12 + 6 columns here instead of 16 + 2.)
+__host__ __device__ __forceinline__ int adj_cpl(int n, int CG) {
+  int np = (n + CG * ADJ_CPL - 1) / (CG * ADJ_CPL);
+  np = np < 1 ? 1 : np;
+  const int cpl = (n + CG * np - 1) / (CG * np);
+  return cpl < 1 ? 1 : (cpl > ADJ_CPL ? ADJ_CPL : cpl);
+}
+
 // Column passes of a task for the warp routine below (per_pass columns
 // each): the batch splits wide tasks into work items by pass.
 __host__ __device__ __forceinline__ int adj_passes(int M, int n) {
   const int CG = 32 / (M <= 8 ? 2 : (M <= 32 ? 4 : 8));
-  int cpl = (n + CG - 1) / CG;
-  cpl = cpl < 1 ? 1 : (cpl > ADJ_CPL ? ADJ_CPL : cpl);
-  const int per_pass = CG * cpl;
+  const int per_pass = CG * adj_cpl(n, CG);
   return (n + per_pass - 1) / per_pass;
 }
 
@@ -142,7 +152,7 @@ __device__ void adj_task_warp(const DTask& t, const FT* __restrict__ A,
   const int rg = lane % RG, cg = lane / RG;
   const int32_t* __restrict__ rmap = maps + t.rmap_off;
   const int32_t* __restrict__ cmap = maps + t.cmap_off;
-  const int cpl = min(ADJ_CPL, (t.n + CG - 1) / CG);
+  const int cpl = adj_cpl(t.n, CG);
   const int per_pass = CG * cpl;
   // the task's input entries are staged once when they fit
   const bool staged = t.M <= ADJ_VS;
