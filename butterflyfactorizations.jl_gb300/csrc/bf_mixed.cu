@@ -515,7 +515,7 @@ static int mixed_setup(Operator& op) {
       ms->stage_mnp[s] += Mb * nb * 64;
     }
   ms->F_bytes = off;
-  // work units: (task, first output block, output blocks), largest first per stage
+  // work units: (task, first output block, output blocks), largest task first per stage
   std::vector<int4> units;
   auto make_units = [&](bool adj, std::vector<int64_t>& beg) {
     beg.assign(ns + 1, 0);
@@ -527,11 +527,14 @@ static int mixed_setup(Operator& op) {
         if (t.kind != TASK_DENSE) continue;
         const int Mb = (t.M + 7) / 8, nb = (t.n + 7) / 8;
         const int nout_b = adj ? nb : Mb, nin_b = adj ? Mb : nb;
-        for (int o = 0; o < nout_b; o += MX_OB) {
-          const int no = std::min(MX_OB, nout_b - o);
-          const int64_t work = (int64_t)((nin_b + MX_IB - 1) / MX_IB) * (4 + no);
-          us.push_back({work, make_int4((int)ti, o, no, 0)});
-        }
+        // the units of one task share its input rows: keyed by the task's work they
+        // stay next to each other in the queue, so the second unit's gathers find
+        // the rows the first one just brought into L2
+        int64_t work = 0;
+        for (int o = 0; o < nout_b; o += MX_OB)
+          work += (int64_t)((nin_b + MX_IB - 1) / MX_IB) * (4 + std::min(MX_OB, nout_b - o));
+        for (int o = 0; o < nout_b; o += MX_OB)
+          us.push_back({work, make_int4((int)ti, o, std::min(MX_OB, nout_b - o), 0)});
       }
       std::stable_sort(us.begin(), us.end(),
                        [](const auto& a, const auto& b) { return a.first > b.first; });
