@@ -400,6 +400,21 @@ def run_rows(args, rank, world, local):
         t_load = time.perf_counter() - t0
         same = bool(np.array_equal(back.matvec(x), y0))
         del back
+    # materialised adjoint of the same operator against its adjoint view
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.zeros_like(xd)
+    stream = torch.cuda.Stream()
+    t0 = time.perf_counter()
+    cop = op.adjoint_copy()
+    t_copy = time.perf_counter() - t0
+    ms_view = time_plain(op.adjoint(), xd, yd, n2, stream, 10, 3)
+    ms_copy = time_plain(cop, xd, yd, n2, stream, 10, 3)
+    ya = op.adjoint().matvec(x)
+    line["adjoint_copy"] = {
+        "operator": "sphere65k far field, complex FP32 factors", "copy_s": t_copy,
+        "adjoint_view_ms": ms_view, "copy_forward_ms": ms_copy, "speedup": ms_view / ms_copy,
+        "rel_diff": float(np.linalg.norm(cop.matvec(x) - ya) / np.linalg.norm(ya))}
+    del cop
     line["persisted"] = {"operator": "sphere65k far field, complex FP32 factors",
                          "file_bytes": int(size), "save_s": t_save, "load_s": t_load,
                          "save_gbs": size / t_save / 1e9, "load_gbs": size / t_load / 1e9,

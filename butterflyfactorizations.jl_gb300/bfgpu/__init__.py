@@ -404,6 +404,14 @@ class Operator:
         check(load().bf_op_recompress(self._h, float(tau), C.byref(h)), "bf_op_recompress")
         return Operator(h.value, self.ctx)
 
+    def adjoint_copy(self, trans: int = BF_OP_C) -> "Operator":
+        """The reference's materialised ``adjoint(BF)`` (``trans=BF_OP_C``) or
+        ``transpose(BF)`` (``BF_OP_T``) of every far block (``bf_op_adjoint_copy``): a new
+        operator whose forward product is op(A) x."""
+        h = C.c_void_p()
+        check(load().bf_op_adjoint_copy(self._h, int(trans), C.byref(h)), "bf_op_adjoint_copy")
+        return Operator(h.value, self.ctx)
+
     def save(self, path: str):
         """Write the operator to ``path`` (``bf_op_save``): packed layout and factors."""
         check(load().bf_op_save(self._h, os.fsencode(path)), "bf_op_save")

@@ -103,6 +103,7 @@ SIGNATURES = [
     ("bf_op_mixed_info", C.c_int, [vp, P(i64), P(i64), P(i64)]),
     ("bf_op_task_shapes", C.c_int, [vp, P(i64), P(i32), P(i32), P(i32), P(i32)]),
     ("bf_op_recompress", C.c_int, [vp, f64, P(vp)]),
+    ("bf_op_adjoint_copy", C.c_int, [vp, C.c_int, P(vp)]),
     ("bf_op_save", C.c_int, [vp, C.c_char_p]),
     ("bf_op_load", C.c_int, [vp, C.c_char_p, P(vp)]),
     ("bf_op_destroy", C.c_int, [vp]),

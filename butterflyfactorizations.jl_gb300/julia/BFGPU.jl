@@ -321,6 +321,22 @@ function recompress_BF(A::GPUButterflyOperator, tau::Real)
 end
 
 """
+    adjoint_copy(A) / transpose_copy(A)
+
+The reference's materialised adjoint(BF) / transpose(BF)
+(src/Butterflyalgebra/bfadjtr.jl:43-67) over every far block
+(bf_op_adjoint_copy): a new operator applied by the forward kernels.
+"""
+function _adjoint_copy(A::GPUButterflyOperator, trans::Integer)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:bf_op_adjoint_copy, lib), Cint, (Ptr{Cvoid}, Cint, Ref{Ptr{Cvoid}}),
+                A.h, Cint(trans), h), "bf_op_adjoint_copy")
+    return _wrap(h[])
+end
+adjoint_copy(A::GPUButterflyOperator) = _adjoint_copy(A, 1)
+transpose_copy(A::GPUButterflyOperator) = _adjoint_copy(A, 2)
+
+"""
     save(A::GPUButterflyOperator, path) / load(ctx, path)
 
 A built operator to a file and back (bf_op_save / bf_op_load): a second run

@@ -433,6 +433,16 @@ BF_API int bf_op_task_shapes(bf_op_t op, int64_t* n_tasks, int32_t* stage, int32
  * refused (BF_ENOTSUP). */
 BF_API int bf_op_recompress(bf_op_t op, double tau, bf_op_t* out);
 
+/* Materialised adjoint (trans = BF_OP_C) or transpose (BF_OP_T): a new
+ * operator whose forward matvec is op(A) x, as the reference's adjoint(BF) /
+ * transpose(BF) (src/Butterflyalgebra/bfadjtr.jl:13-67) build one: blocks
+ * conjugate-transposed (transposed) with swapped routing keys, R levels
+ * reversed, Q and P exchanged, the trees swapped.  The factor storage is kept.
+ * bf_matvec's BF_OP_C / BF_OP_T views need no copy; the copy runs at the
+ * forward kernels' speed for twice the factor memory.  Operators with a near
+ * field are refused (BF_ENOTSUP). */
+BF_API int bf_op_adjoint_copy(bf_op_t op, int trans, bf_op_t* out);
+
 /* Persisted operators (no reference counterpart: the reference keeps its
  * factors in memory only and rebuilds them with every assemble_BF,
  * src/ButterflyFactorization/bfassembly.jl:48-200).  bf_op_save writes the
