@@ -124,11 +124,12 @@ class Tree:
 
 
 def nearandfar(tree_o: Tree, tree_s: Tree, alpha: float = 1.0, minbflvl: int = 3,
-               leafcomp: bool = True, leafimbalance: bool = True):
+               leafcomp: bool = True, leafimbalance: bool = True, unbalancedints: bool = False):
     """Far pairs (n_far, 2) [observer node, source node] and the near-pair count."""
     lib = load()
     nf, nn = C.c_int64(), C.c_int64()
-    args = (tree_o._h, tree_s._h, float(alpha), int(minbflvl), int(leafcomp), int(leafimbalance))
+    args = (tree_o._h, tree_s._h, float(alpha), int(minbflvl), int(leafcomp), int(leafimbalance),
+            int(unbalancedints))
     check(lib.bf_nearandfar(*args, None, None, 0, C.byref(nf), C.byref(nn)), "bf_nearandfar")
     fo = np.zeros(max(nf.value, 1), np.int64)
     fs = np.zeros(max(nf.value, 1), np.int64)
@@ -138,11 +139,12 @@ def nearandfar(tree_o: Tree, tree_s: Tree, alpha: float = 1.0, minbflvl: int = 3
 
 
 def near_pairs(tree_o: Tree, tree_s: Tree, alpha: float = 1.0, minbflvl: int = 3,
-               leafcomp: bool = True, leafimbalance: bool = True):
+               leafcomp: bool = True, leafimbalance: bool = True, unbalancedints: bool = False):
     """Near pairs (n_near, 2) [observer node, source node] of the same traversal."""
     lib = load()
     nn = C.c_int64()
-    args = (tree_o._h, tree_s._h, float(alpha), int(minbflvl), int(leafcomp), int(leafimbalance))
+    args = (tree_o._h, tree_s._h, float(alpha), int(minbflvl), int(leafcomp), int(leafimbalance),
+            int(unbalancedints))
     check(lib.bf_near_pairs(*args, None, None, 0, C.byref(nn)), "bf_near_pairs")
     fo = np.zeros(max(nn.value, 1), np.int64)
     fs = np.zeros(max(nn.value, 1), np.int64)
@@ -152,14 +154,15 @@ def near_pairs(tree_o: Tree, tree_s: Tree, alpha: float = 1.0, minbflvl: int = 3
 
 
 def nearandfar_gpu(tree_o: Tree, tree_s: Tree, alpha: float = 1.0, minbflvl: int = 3,
-                   leafcomp: bool = True, leafimbalance: bool = True, ctx=None):
+                   leafcomp: bool = True, leafimbalance: bool = True,
+                   unbalancedints: bool = False, ctx=None):
     """Far and near pairs, (n, 2) arrays each, traversed on the GPU (same order as
     ``nearandfar`` / ``near_pairs``)."""
     lib = load()
     ctx = ctx or default_context()
     nf, nn = C.c_int64(), C.c_int64()
     args = (ctx._h, tree_o._h, tree_s._h, float(alpha), int(minbflvl), int(leafcomp),
-            int(leafimbalance))
+            int(leafimbalance), int(unbalancedints))
     check(lib.bf_nearandfar_gpu(*args, None, None, 0, None, None, 0, C.byref(nf), C.byref(nn)),
           "bf_nearandfar_gpu")
     a = [np.zeros(max(v, 1), np.int64) for v in (nf.value, nf.value, nn.value, nn.value)]
@@ -381,11 +384,12 @@ class Operator:
 
     def add_near(self, obs, src, tree_o: Tree, tree_s: Tree, k: float, pairs=None,
                  alpha: float = 1.0, minbflvl: int = 3, leafcomp: bool = True,
-                 leafimbalance: bool = True):
+                 leafimbalance: bool = True, unbalancedints: bool = False):
         """Attach the near field (``bf_op_add_near``): afterwards every matvec applies
         near + far, as the reference's ``mul!`` on a full ``PetrovGalerkinBF``."""
         if pairs is None:
-            pairs = near_pairs(tree_o, tree_s, alpha, minbflvl, leafcomp, leafimbalance)
+            pairs = near_pairs(tree_o, tree_s, alpha, minbflvl, leafcomp, leafimbalance,
+                               unbalancedints)
         obs = np.ascontiguousarray(obs, np.float64)
         src = np.ascontiguousarray(src, np.float64)
         pairs = np.asarray(pairs, np.int64).reshape(-1, 2)
@@ -561,14 +565,18 @@ def PetrovGalerkinBF(obs, src, tree_o: Tree, tree_s: Tree, k: float, tol: float 
                      min_samples: int = 10, rank_mode: int = 0, surrogate=None,
                      keep_mixed: bool = True, ctx: Context | None = None,
                      factor_storage: int = BF_STORE_C32,
-                     farfieldonly: bool = True, leafimbalance: bool = True) -> Operator:
+                     farfieldonly: bool = True, leafimbalance: bool = True,
+                     unbalancedints: bool = False) -> Operator:
     """``PetrovGalerkinBF`` on the GPU: the far field (``farfieldonly=True``, the default
     here) or near + far (``farfieldonly=False``, the reference's default; the near blocks
-    leave out the singular self-term r = 0)."""
-    far, _ = nearandfar(tree_o, tree_s, alpha, minbflvl, leafcomp, leafimbalance)
+    leave out the singular self-term r = 0).  ``unbalancedints``: the traversal splits only
+    the larger node of a pair (``intlists.jl:121-149``)."""
+    far, _ = nearandfar(tree_o, tree_s, alpha, minbflvl, leafcomp, leafimbalance,
+                        unbalancedints)
     op = _build(obs, src, tree_o, tree_s, far, k, tol, c_tau, adaptive, seed, min_samples,
                 rank_mode, surrogate, keep_mixed, ctx, factor_storage)
     if not farfieldonly:
         op.add_near(obs, src, tree_o, tree_s, k, alpha=alpha, minbflvl=minbflvl,
-                    leafcomp=leafcomp, leafimbalance=leafimbalance)
+                    leafcomp=leafcomp, leafimbalance=leafimbalance,
+                    unbalancedints=unbalancedints)
     return op

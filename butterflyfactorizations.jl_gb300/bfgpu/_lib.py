@@ -63,11 +63,11 @@ SIGNATURES = [
     ("bf_tree_export", C.c_int, [vp, P(f64), P(f64), P(i32), P(i32), P(i32), P(i32), P(i64),
                                  P(i64), P(i64)]),
     ("bf_tree_destroy", C.c_int, [vp]),
-    ("bf_nearandfar", C.c_int, [vp, vp, f64, i32, i32, i32, P(i64), P(i64), i64, P(i64),
+    ("bf_nearandfar", C.c_int, [vp, vp, f64, i32, i32, i32, i32, P(i64), P(i64), i64, P(i64),
                                 P(i64)]),
-    ("bf_near_pairs", C.c_int, [vp, vp, f64, i32, i32, i32, P(i64), P(i64), i64, P(i64)]),
+    ("bf_near_pairs", C.c_int, [vp, vp, f64, i32, i32, i32, i32, P(i64), P(i64), i64, P(i64)]),
     ("bf_tree_build_gpu", C.c_int, [vp, P(f64), i64, i32, i32, P(vp)]),
-    ("bf_nearandfar_gpu", C.c_int, [vp, vp, vp, f64, i32, i32, i32, P(i64), P(i64), i64, P(i64),
+    ("bf_nearandfar_gpu", C.c_int, [vp, vp, vp, f64, i32, i32, i32, i32, P(i64), P(i64), i64, P(i64),
                                     P(i64), i64, P(i64), P(i64)]),
     ("bf_build_opts_default", None, [P(BuildOpts)]),
     ("bf_train_opts_default", None, [P(TrainOpts)]),

@@ -160,7 +160,7 @@ std::vector<std::vector<int64_t>> traverse_and_pad(const Tree& t, int64_t root);
 bool is_far(const Tree& ts, const Tree& to, int64_t snode, int64_t onode, double alpha);
 // far and near pairs of the dual-tree traversal (src/Matrixassembly/intlists.jl:30-217)
 void near_far_lists(const Tree& to, const Tree& ts, double alpha, int32_t minbflvl,
-                    int32_t leafcomp, int32_t leafimbalance,
+                    int32_t leafcomp, int32_t leafimbalance, int32_t unbalancedints,
                     std::vector<std::pair<int64_t, int64_t>>* far,
                     std::vector<std::pair<int64_t, int64_t>>* near, int64_t* n_far,
                     int64_t* n_near);

@@ -259,7 +259,7 @@ namespace bfg {
 // pairs go to `far` (when given), near pairs to `near` (when given); both
 // are always counted.
 void near_far_lists(const Tree& to, const Tree& ts, double alpha, int32_t minbflvl,
-                    int32_t leafcomp, int32_t leafimbalance,
+                    int32_t leafcomp, int32_t leafimbalance, int32_t unbalancedints,
                     std::vector<std::pair<int64_t, int64_t>>* far,
                     std::vector<std::pair<int64_t, int64_t>>* near, int64_t* n_far,
                     int64_t* n_near) {
@@ -299,7 +299,13 @@ void near_far_lists(const Tree& to, const Tree& ts, double alpha, int32_t minbfl
       continue;
     }
     kids.clear();
-    if (lo) {
+    if (unbalancedints) {  // only the larger node splits (intlists.jl:121-149)
+      if ((to.radius(it.o) >= ts.radius(it.s) && !lo) || ls) {
+        for (int32_t c = 0; c < to.n_child[it.o]; ++c) kids.push_back({to.first_child[it.o] + c, it.s, it.h - 1});
+      } else {
+        for (int32_t c = 0; c < ts.n_child[it.s]; ++c) kids.push_back({it.o, ts.first_child[it.s] + c, it.h - 1});
+      }
+    } else if (lo) {
       for (int32_t c = 0; c < ts.n_child[it.s]; ++c) kids.push_back({it.o, ts.first_child[it.s] + c, it.h - 1});
     } else if (ls) {
       for (int32_t c = 0; c < to.n_child[it.o]; ++c) kids.push_back({to.first_child[it.o] + c, it.s, it.h - 1});
@@ -319,7 +325,8 @@ void near_far_lists(const Tree& to, const Tree& ts, double alpha, int32_t minbfl
 extern "C" {
 
 int bf_nearandfar(bf_tree_t obs_tree, bf_tree_t src_tree, double alpha, int32_t minbflvl,
-                  int32_t leafcomp, int32_t leafimbalance, int64_t* far_obs, int64_t* far_src,
+                  int32_t leafcomp, int32_t leafimbalance, int32_t unbalancedints,
+                  int64_t* far_obs, int64_t* far_src,
                   int64_t capacity, int64_t* n_far, int64_t* n_near) {
   if (!obs_tree || !src_tree) {
     set_error("bf_nearandfar: NULL tree");
@@ -328,7 +335,7 @@ int bf_nearandfar(bf_tree_t obs_tree, bf_tree_t src_tree, double alpha, int32_t 
   std::vector<std::pair<int64_t, int64_t>> far;
   int64_t nf = 0, nn = 0;
   near_far_lists(obs_tree->t, src_tree->t, alpha, minbflvl, leafcomp, leafimbalance,
-                 (far_obs && far_src) ? &far : nullptr, nullptr, &nf, &nn);
+                 unbalancedints, (far_obs && far_src) ? &far : nullptr, nullptr, &nf, &nn);
   if (n_far) *n_far = nf;
   if (n_near) *n_near = nn;
   if (capacity > 0 && nf > capacity) {
@@ -343,7 +350,8 @@ int bf_nearandfar(bf_tree_t obs_tree, bf_tree_t src_tree, double alpha, int32_t 
 }
 
 int bf_near_pairs(bf_tree_t obs_tree, bf_tree_t src_tree, double alpha, int32_t minbflvl,
-                  int32_t leafcomp, int32_t leafimbalance, int64_t* near_obs, int64_t* near_src,
+                  int32_t leafcomp, int32_t leafimbalance, int32_t unbalancedints,
+                  int64_t* near_obs, int64_t* near_src,
                   int64_t capacity, int64_t* n_near) {
   if (!obs_tree || !src_tree) {
     set_error("bf_near_pairs: NULL tree");
@@ -351,8 +359,8 @@ int bf_near_pairs(bf_tree_t obs_tree, bf_tree_t src_tree, double alpha, int32_t 
   }
   std::vector<std::pair<int64_t, int64_t>> near;
   int64_t nn = 0;
-  near_far_lists(obs_tree->t, src_tree->t, alpha, minbflvl, leafcomp, leafimbalance, nullptr,
-                 (near_obs && near_src) ? &near : nullptr, nullptr, &nn);
+  near_far_lists(obs_tree->t, src_tree->t, alpha, minbflvl, leafcomp, leafimbalance,
+                 unbalancedints, nullptr, (near_obs && near_src) ? &near : nullptr, nullptr, &nn);
   if (n_near) *n_near = nn;
   if (capacity > 0 && nn > capacity) {
     set_error("bf_near_pairs: capacity %lld < %lld near pairs", (long long)capacity,

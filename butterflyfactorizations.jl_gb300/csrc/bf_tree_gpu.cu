@@ -270,12 +270,20 @@ __device__ bool is_far_dev(const TreeDev& ts, const TreeDev& to, int s, int o, d
   return __dsqrt_rn(mind_sq) > target;
 }
 
+// unbalanced splitting: the observer node splits when it is the larger one
+// (largernode: radius(o) >= radius(s), treeinterface.jl:153-154) and not a
+// leaf, or when the source node is a leaf
+__device__ __forceinline__ bool split_obs(const TreeDev& to, const TreeDev& ts, int o, int s,
+                                          bool lo, bool ls, double sqrt3) {
+  return (__dmul_rn(to.half[o], sqrt3) >= __dmul_rn(ts.half[s], sqrt3) && !lo) || ls;
+}
+
 // classify every pair of a level: flags far / near, kid count
 __global__ void classify_kernel(const int32_t* __restrict__ po, const int32_t* __restrict__ ps,
                                 int64_t n, TreeDev to, TreeDev ts, int h, double alpha,
                                 double sqrt3, int minbflvl, int leafcomp, int leafimbalance,
-                                int32_t* __restrict__ is_far, int32_t* __restrict__ is_near,
-                                int32_t* __restrict__ nkids) {
+                                int unbal, int32_t* __restrict__ is_far,
+                                int32_t* __restrict__ is_near, int32_t* __restrict__ nkids) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int o = po[i], s = ps[i];
@@ -290,6 +298,8 @@ __global__ void classify_kernel(const int32_t* __restrict__ po, const int32_t* _
         f = 1;
     } else if ((lo && ls) || ((lo || ls) && !leafimbalance)) {
       nr = 1;
+    } else if (unbal) {  // only the larger node splits (intlists.jl:121-149)
+      k = split_obs(to, ts, o, s, lo, ls, sqrt3) ? to.n_child[o] : ts.n_child[s];
     } else {
       k = lo ? ts.n_child[s] : (ls ? to.n_child[o] : to.n_child[o] * ts.n_child[s]);
     }
@@ -302,7 +312,8 @@ __global__ void classify_kernel(const int32_t* __restrict__ po, const int32_t* _
 // outputs of the level at their positions; kids into the next frontier in order
 __global__ void expand_kernel(const int32_t* __restrict__ po, const int32_t* __restrict__ ps,
                               const PairKey* __restrict__ pk, int64_t n, int L, TreeDev to,
-                              TreeDev ts, const int32_t* __restrict__ is_far,
+                              TreeDev ts, int unbal, double sqrt3,
+                              const int32_t* __restrict__ is_far,
                               const int32_t* __restrict__ is_near,
                               const int32_t* __restrict__ nkids, const int64_t* __restrict__ far_pos,
                               const int64_t* __restrict__ near_pos,
@@ -326,10 +337,14 @@ __global__ void expand_kernel(const int32_t* __restrict__ po, const int32_t* __r
     } else if (nkids[i] > 0) {
       const bool lo = to.n_child[o] == 0, ls = ts.n_child[s] == 0;
       const int nco = to.n_child[o], ncs = ts.n_child[s];
+      const bool so = unbal && split_obs(to, ts, o, s, lo, ls, sqrt3);
       int64_t q = kid_pos[i];
       for (int j = 0; j < nkids[i]; ++j, ++q) {
         int co, cs;
-        if (lo) {
+        if (unbal) {
+          co = so ? to.first_child[o] + j : o;
+          cs = so ? s : ts.first_child[s] + j;
+        } else if (lo) {
           co = o;
           cs = ts.first_child[s] + j;
         } else if (ls) {
@@ -542,7 +557,8 @@ extern "C" int bf_tree_build_gpu(bf_ctx_t ctx, const double* xyz, int64_t n, int
 
 extern "C" int bf_nearandfar_gpu(bf_ctx_t ctx, bf_tree_t obs_tree, bf_tree_t src_tree,
                                  double alpha, int32_t minbflvl, int32_t leafcomp,
-                                 int32_t leafimbalance, int64_t* far_obs, int64_t* far_src,
+                                 int32_t leafimbalance, int32_t unbalancedints,
+                                 int64_t* far_obs, int64_t* far_src,
                                  int64_t far_capacity, int64_t* near_obs, int64_t* near_src,
                                  int64_t near_capacity, int64_t* n_far, int64_t* n_near) {
   try {
@@ -619,7 +635,7 @@ extern "C" int bf_nearandfar_gpu(bf_ctx_t ctx, bf_tree_t obs_tree, bf_tree_t src
       BF_TRY(mem.get(&sums, ntile, "bf_nearandfar_gpu"));
       classify_kernel<<<grid_of(nfront), 256, 0, st>>>(po, ps, nfront, dto, dts, h0 - L, alpha,
                                                        sqrt3, minbflvl, leafcomp, leafimbalance,
-                                                       isf, isn, nk);
+                                                       unbalancedints ? 1 : 0, isf, isn, nk);
       BF_TRY_CUDA(cudaGetLastError());
       int64_t nf = 0, nn = 0, nkid = 0;
       BF_TRY(exclusive_scan(isf, nfront, fpos, sums, d_total, &nf, st));
@@ -639,7 +655,8 @@ extern "C" int bf_nearandfar_gpu(bf_ctx_t ctx, bf_tree_t obs_tree, bf_tree_t src
       BF_TRY(mem.get(&qo, nkid, "bf_nearandfar_gpu"));
       BF_TRY(mem.get(&qs, nkid, "bf_nearandfar_gpu"));
       BF_TRY(mem.get(&qk, nkid, "bf_nearandfar_gpu"));
-      expand_kernel<<<grid_of(nfront), 256, 0, st>>>(po, ps, pk, nfront, L, dto, dts, isf, isn,
+      expand_kernel<<<grid_of(nfront), 256, 0, st>>>(po, ps, pk, nfront, L, dto, dts,
+                                                     unbalancedints ? 1 : 0, sqrt3, isf, isn,
                                                      nk, fpos, npos, kpos, lo.fo, lo.fs, lo.fk,
                                                      lo.no, lo.ns, lo.nk, qo, qs, qk);
       BF_TRY_CUDA(cudaGetLastError());

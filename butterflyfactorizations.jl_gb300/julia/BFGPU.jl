@@ -221,13 +221,13 @@ traversal of src/Matrixassembly/intlists.jl:30-217 with the AABB isFarFunctor
 of ext/BFH2Trees/h2admissible.jl:11-45.
 """
 function nearandfar_gpu(to::GPUTree, ts::GPUTree; alpha=1.0, minbflvl=3, leafcomp=true,
-                        leafimbalance=true)
+                        leafimbalance=true, unbalancedints=false)
     nf = Ref{Int64}(0); nn = Ref{Int64}(0)
     args(fo, fs, cap) = ccall((:bf_nearandfar, lib), Cint,
-                              (Ptr{Cvoid}, Ptr{Cvoid}, Float64, Int32, Int32, Int32, Ptr{Int64},
-                               Ptr{Int64}, Int64, Ref{Int64}, Ref{Int64}),
-                              to.h, ts.h, alpha, minbflvl, leafcomp, leafimbalance, fo, fs, cap,
-                              nf, nn)
+                              (Ptr{Cvoid}, Ptr{Cvoid}, Float64, Int32, Int32, Int32, Int32,
+                               Ptr{Int64}, Ptr{Int64}, Int64, Ref{Int64}, Ref{Int64}),
+                              to.h, ts.h, alpha, minbflvl, leafcomp, leafimbalance,
+                              unbalancedints, fo, fs, cap, nf, nn)
     check(args(C_NULL, C_NULL, 0), "bf_nearandfar")
     fo = zeros(Int64, max(nf[], 1)); fs = zeros(Int64, max(nf[], 1))
     check(args(fo, fs, length(fo)), "bf_nearandfar")
@@ -257,13 +257,13 @@ end
 Near pairs (library node ids, 0-based) of the same traversal as nearandfar_gpu.
 """
 function near_pairs_gpu(to::GPUTree, ts::GPUTree; alpha=1.0, minbflvl=3, leafcomp=true,
-                        leafimbalance=true)
+                        leafimbalance=true, unbalancedints=false)
     nn = Ref{Int64}(0)
     args(no, ns, cap) = ccall((:bf_near_pairs, lib), Cint,
-                              (Ptr{Cvoid}, Ptr{Cvoid}, Float64, Int32, Int32, Int32, Ptr{Int64},
-                               Ptr{Int64}, Int64, Ref{Int64}),
-                              to.h, ts.h, alpha, minbflvl, leafcomp, leafimbalance, no, ns, cap,
-                              nn)
+                              (Ptr{Cvoid}, Ptr{Cvoid}, Float64, Int32, Int32, Int32, Int32,
+                               Ptr{Int64}, Ptr{Int64}, Int64, Ref{Int64}),
+                              to.h, ts.h, alpha, minbflvl, leafcomp, leafimbalance,
+                              unbalancedints, no, ns, cap, nn)
     check(args(C_NULL, C_NULL, 0), "bf_near_pairs")
     no = zeros(Int64, max(nn[], 1)); ns = zeros(Int64, max(nn[], 1))
     check(args(no, ns, length(no)), "bf_near_pairs")
@@ -272,8 +272,8 @@ end
 
 """
     PetrovGalerkinBF(HelmholtzPoints(), X, Y, tree, k; tol=1e-3, alpha=1.0, Ctau=2.9592,
-                     minbflvl=3, leafcomp=true, leafimbalance=true, adaptive=true,
-                     farfieldonly=false, storage=:c32, ctx=Context(0))
+                     minbflvl=3, leafcomp=true, leafimbalance=true, unbalancedints=false,
+                     adaptive=true, farfieldonly=false, storage=:c32, ctx=Context(0))
 
 The reference's PetrovGalerkinBF (petrovgalerkinbf.jl:33-54) built on the GPU:
 the trees of `tree` (cluster_testtree / cluster_trialtree) are converted, the
@@ -287,15 +287,15 @@ factors as 16-byte float-float entries.
 function PetrovGalerkinBF(::HelmholtzPoints, X::AbstractMatrix{Float64},
                           Y::AbstractMatrix{Float64}, tree, k::Float64; tol=1e-3, alpha=1.0,
                           Ctau=2.9592, minbflvl=3, leafcomp=true, leafimbalance=true,
-                          adaptive=true, farfieldonly=false, seed=0, min_samples=10,
-                          storage=:c32, ctx::Context=Context(0))
+                          unbalancedints=false, adaptive=true, farfieldonly=false, seed=0,
+                          min_samples=10, storage=:c32, ctx::Context=Context(0))
     to = GPUTree(cluster_testtree(tree), size(X, 2))
     ts = GPUTree(cluster_trialtree(tree), size(Y, 2))
-    fo, fs, _ = nearandfar_gpu(to, ts; alpha, minbflvl, leafcomp, leafimbalance)
+    fo, fs, _ = nearandfar_gpu(to, ts; alpha, minbflvl, leafcomp, leafimbalance, unbalancedints)
     A = _build(ctx, X, Y, to, ts, fo, fs, k, tol; c_tau=Ctau, adaptive=Int32(adaptive),
                seed=UInt64(seed), min_samples=Int32(min_samples), storage)
     if !farfieldonly
-        no, ns = near_pairs_gpu(to, ts; alpha, minbflvl, leafcomp, leafimbalance)
+        no, ns = near_pairs_gpu(to, ts; alpha, minbflvl, leafcomp, leafimbalance, unbalancedints)
         x = Matrix{Float64}(X); y = Matrix{Float64}(Y)
         check(ccall((:bf_op_add_near, lib), Cint,
                     (Ptr{Cvoid}, Ptr{Float64}, Int64, Ptr{Float64}, Int64, Ptr{Cvoid},

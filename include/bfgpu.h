@@ -96,12 +96,14 @@ BF_API int bf_tree_export(bf_tree_t tree, double* center, double* halfsize, int3
 BF_API int bf_tree_destroy(bf_tree_t tree);
 
 /* Near/far interaction lists: src/Matrixassembly/intlists.jl:30-217 with the
- * AABB isFarFunctor(alpha) of ext/BFH2Trees/h2admissible.jl:11-45 (balanced
- * splitting).  Call with capacity 0 to query *n_far; pairs are written as
+ * AABB isFarFunctor(alpha) of ext/BFH2Trees/h2admissible.jl:11-45; options as
+ * the reference's nearandfar (minbflvl, leafcomp, leafimbalance, and
+ * unbalancedints: only the larger node of a pair splits, intlists.jl:121-149).
+ * Call with capacity 0 to query *n_far; pairs are written as
  * (far_obs[i], far_src[i]) in the reference's depth-first order. */
 BF_API int bf_nearandfar(bf_tree_t obs_tree, bf_tree_t src_tree, double alpha,
                          int32_t minbflvl, int32_t leafcomp, int32_t leafimbalance,
-                         int64_t* far_obs, int64_t* far_src, int64_t capacity,
+                         int32_t unbalancedints, int64_t* far_obs, int64_t* far_src, int64_t capacity,
                          int64_t* n_far, int64_t* n_near);
 
 /* The same tree and interaction lists, built on the GPU (the reference builds
@@ -117,7 +119,7 @@ BF_API int bf_tree_build_gpu(bf_ctx_t ctx, const double* xyz, int64_t n_points,
                              int32_t max_points, int32_t max_depth, bf_tree_t* out);
 BF_API int bf_nearandfar_gpu(bf_ctx_t ctx, bf_tree_t obs_tree, bf_tree_t src_tree, double alpha,
                              int32_t minbflvl, int32_t leafcomp, int32_t leafimbalance,
-                             int64_t* far_obs, int64_t* far_src, int64_t far_capacity,
+                             int32_t unbalancedints, int64_t* far_obs, int64_t* far_src, int64_t far_capacity,
                              int64_t* near_obs, int64_t* near_src, int64_t near_capacity,
                              int64_t* n_far, int64_t* n_near);
 
@@ -125,7 +127,7 @@ BF_API int bf_nearandfar_gpu(bf_ctx_t ctx, bf_tree_t obs_tree, bf_tree_t src_tre
  * (near_obs[i], near_src[i]) in depth-first order; capacity 0 queries *n_near. */
 BF_API int bf_near_pairs(bf_tree_t obs_tree, bf_tree_t src_tree, double alpha,
                          int32_t minbflvl, int32_t leafcomp, int32_t leafimbalance,
-                         int64_t* near_obs, int64_t* near_src, int64_t capacity,
+                         int32_t unbalancedints, int64_t* near_obs, int64_t* near_src, int64_t capacity,
                          int64_t* n_near);
 
 /* ------------------------------------------------------------------------

@@ -268,8 +268,10 @@ def is_far(tree_s: Tree, tree_o: Tree, snode: int, onode: int, alpha: float) -> 
 
 
 def nearandfar(tree_o: Tree, tree_s: Tree, alpha: float = 1.0, minbflvl: int = 3,
-               leafcomp: bool = True, leafimbalance: bool = True):
-    """Dual-tree traversal ``src/Matrixassembly/intlists.jl:30-217`` (balanced splitting).
+               leafcomp: bool = True, leafimbalance: bool = True, unbalancedints: bool = False):
+    """Dual-tree traversal ``src/Matrixassembly/intlists.jl:30-217``: balanced splitting,
+    or with ``unbalancedints`` only the larger node of a pair splits (``:121-149``,
+    ``largernode`` = radius comparison, ``src/treeinterface.jl:153-154``).
 
     Returns ``(far, near)`` lists of ``(observer_node, source_node)`` in the
     reference's depth-first order.
@@ -295,7 +297,12 @@ def nearandfar(tree_o: Tree, tree_s: Tree, alpha: float = 1.0, minbflvl: int = 3
             near.append((no, ns))
             continue
         kids = []
-        if lo:
+        if unbalancedints:
+            if (tree_o.radius(no) >= tree_s.radius(ns) and not lo) or ls:
+                kids = [(co, ns) for co in tree_o.children(no)]
+            else:
+                kids = [(no, cs) for cs in tree_s.children(ns)]
+        elif lo:
             kids = [(no, cs) for cs in tree_s.children(ns)]
         elif ls:
             kids = [(co, ns) for co in tree_o.children(no)]
@@ -800,13 +807,15 @@ class FarOperator:
 
 def assemble_far(kern, tree_o: Tree, tree_s: Tree, k: float, tol: float, alpha: float = 1.0,
                  c_tau: float = 2.9592, adaptive: bool = True, seed: int = 0,
-                 minbflvl: int = 3, log: list | None = None) -> FarOperator:
+                 minbflvl: int = 3, log: list | None = None,
+                 unbalancedints: bool = False) -> FarOperator:
     """One ``assemble_BF`` per admissible pair (``petrovgalerkinbf.jl:129-151``).
 
     ``c_tau = 2.9592`` is the TwoNTree + isFarFunctor constant
     (``ext/BFH2Trees/h2parameters.jl:44-48``) that ``PetrovGalerkinBF`` uses.
     """
-    far, _ = nearandfar(tree_o, tree_s, alpha=alpha, minbflvl=minbflvl)
+    far, _ = nearandfar(tree_o, tree_s, alpha=alpha, minbflvl=minbflvl,
+                        unbalancedints=unbalancedints)
     bfs = [assemble_bf(kern, tree_o, tree_s, no, ns, k, tol, c_tau, adaptive, seed, i, log=log)
            for i, (no, ns) in enumerate(far)]
     return FarOperator(bfs, far, len(tree_o.perm), len(tree_s.perm))

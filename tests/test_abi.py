@@ -74,7 +74,8 @@ def test_tree_bit_exact_with_oracle(case):
 
 
 @pytest.mark.parametrize("opts", [dict(leafcomp=False), dict(leafimbalance=False),
-                                  dict(minbflvl=2, leafcomp=False)])
+                                  dict(minbflvl=2, leafcomp=False), dict(unbalancedints=True),
+                                  dict(unbalancedints=True, leafimbalance=False)])
 def test_near_and_far_lists_options(opts):
     """Near and far pairs of the dual traversal under the non-default options
     (intlists.jl:30-217), unbalanced trees: bit-exact with the oracle."""

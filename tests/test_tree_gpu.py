@@ -43,7 +43,8 @@ def test_gpu_tree_and_lists_equal_host(ctx, case):
 
 
 @pytest.mark.parametrize("opts", [dict(), dict(leafcomp=False), dict(leafimbalance=False),
-                                  dict(minbflvl=2, leafcomp=False), dict(alpha=2.0)])
+                                  dict(minbflvl=2, leafcomp=False), dict(alpha=2.0),
+                                  dict(unbalancedints=True)])
 def test_gpu_lists_unbalanced_trees(ctx, opts):
     obs, src = G.plane_pair(3000, 7, z_obs=0.2)
     to, ts = bfgpu.Tree.build(obs, max_points=12), bfgpu.Tree.build(src, max_points=60)
