@@ -35,6 +35,7 @@ from ._lib import (BF_OP_C, BF_OP_N, BF_OP_T, BF_PTR_DEVICE, BF_PTR_HOST, BF_STO
 
 __all__ = ["Tree", "Context", "Operator", "nearandfar", "assemble_BF", "PetrovGalerkinBF",
            "import_blocks", "load_operator", "compress_block", "near_pairs", "nearandfar_gpu", "mul", "BFError",
+           "GeometricRankEstimator",
            "load"]
 
 
@@ -514,8 +515,20 @@ def import_blocks(n_rows, n_cols, bf, stage, obs_out, src_out, obs_in, src_in, r
     return Operator(h.value, ctx)
 
 
+class GeometricRankEstimator:
+    """``GeometricRankEstimator(C, Cε; Rmin=3)`` (``rankestimation.jl:13-25``, tree method
+    ``ext/BFH2Trees/h2rankest.jl:8-38``): sample counts
+    ``max(ceil(C (k a_s a_o / d)^2 + Cε log(1/ε)), Rmin)`` from the node radii and the
+    center distance.  Pass it as ``rank_estimator`` to ``PetrovGalerkinBF`` /
+    ``assemble_BF``; without one the ButterflyRankEstimator(``c_tau``) is used."""
+
+    def __init__(self, C: float = 1.5, Ceps: float = 1.5, Rmin: int = 3):
+        self.C, self.Ceps, self.Rmin = float(C), float(Ceps), int(Rmin)
+
+
 def _build(obs, src, tree_o: Tree, tree_s: Tree, pairs, k, tol, c_tau, adaptive, seed,
-           min_samples, rank_mode, surrogate, keep_mixed, ctx, factor_storage=BF_STORE_C32):
+           min_samples, rank_mode, surrogate, keep_mixed, ctx, factor_storage=BF_STORE_C32,
+           rank_estimator=None):
     lib = load()
     ctx = ctx or default_context()
     obs = np.ascontiguousarray(obs, np.float64)
@@ -532,6 +545,9 @@ def _build(obs, src, tree_o: Tree, tree_s: Tree, pairs, k, tol, c_tau, adaptive,
     o.rank_mode = int(rank_mode)
     o.keep_mixed = int(bool(keep_mixed))
     o.factor_storage = int(factor_storage)
+    if rank_estimator is not None:
+        o.estimator = _lib.BF_EST_GEOMETRIC
+        o.geo_c, o.geo_ceps, o.geo_rmin = rank_estimator.C, rank_estimator.Ceps, rank_estimator.Rmin
     w = None
     if surrogate is not None:
         # a bfgpu.surrogate.RankSurrogate (weights + margin) or a bare weight vector
@@ -551,12 +567,14 @@ def _build(obs, src, tree_o: Tree, tree_s: Tree, pairs, k, tol, c_tau, adaptive,
 def assemble_BF(obs, src, tree_o: Tree, tree_s: Tree, no: int, ns: int, k: float, tau: float,
                 c_tau: float = 4.0, adaptive: bool = True, seed: int = 0, min_samples: int = 10,
                 rank_mode: int = 0, surrogate=None, keep_mixed: bool = True,
-                ctx: Context | None = None, factor_storage: int = BF_STORE_C32) -> Operator:
+                ctx: Context | None = None, factor_storage: int = BF_STORE_C32,
+                rank_estimator: GeometricRankEstimator | None = None) -> Operator:
     """``assemble_BF(kernel, blktree, no, ns, k, tau)`` on the GPU (one far block).
     ``factor_storage``: BF_STORE_C32 (complex FP32, 8 B per entry) or BF_STORE_FF
     (float-float, 16 B per entry, the width of the reference's ComplexF64)."""
     return _build(obs, src, tree_o, tree_s, [(no, ns)], k, tau, c_tau, adaptive, seed,
-                  min_samples, rank_mode, surrogate, keep_mixed, ctx, factor_storage)
+                  min_samples, rank_mode, surrogate, keep_mixed, ctx, factor_storage,
+                  rank_estimator)
 
 
 def PetrovGalerkinBF(obs, src, tree_o: Tree, tree_s: Tree, k: float, tol: float = 1e-3,
@@ -566,7 +584,8 @@ def PetrovGalerkinBF(obs, src, tree_o: Tree, tree_s: Tree, k: float, tol: float 
                      keep_mixed: bool = True, ctx: Context | None = None,
                      factor_storage: int = BF_STORE_C32,
                      farfieldonly: bool = True, leafimbalance: bool = True,
-                     unbalancedints: bool = False) -> Operator:
+                     unbalancedints: bool = False,
+                     rank_estimator: GeometricRankEstimator | None = None) -> Operator:
     """``PetrovGalerkinBF`` on the GPU: the far field (``farfieldonly=True``, the default
     here) or near + far (``farfieldonly=False``, the reference's default; the near blocks
     leave out the singular self-term r = 0).  ``unbalancedints``: the traversal splits only
@@ -574,7 +593,7 @@ def PetrovGalerkinBF(obs, src, tree_o: Tree, tree_s: Tree, k: float, tol: float 
     far, _ = nearandfar(tree_o, tree_s, alpha, minbflvl, leafcomp, leafimbalance,
                         unbalancedints)
     op = _build(obs, src, tree_o, tree_s, far, k, tol, c_tau, adaptive, seed, min_samples,
-                rank_mode, surrogate, keep_mixed, ctx, factor_storage)
+                rank_mode, surrogate, keep_mixed, ctx, factor_storage, rank_estimator)
     if not farfieldonly:
         op.add_near(obs, src, tree_o, tree_s, k, alpha=alpha, minbflvl=minbflvl,
                     leafcomp=leafcomp, leafimbalance=leafimbalance,

@@ -9,6 +9,7 @@ LIB_PATH = os.path.join(_HERE, "libbfgpu.so")
 
 BF_OK, BF_EINVAL, BF_ENOMEM, BF_ECUDA, BF_ETIMEOUT, BF_ENOTSUP, BF_ESTATE = range(7)
 BF_OP_N, BF_OP_C, BF_OP_T = 0, 1, 2
+BF_EST_BUTTERFLY, BF_EST_GEOMETRIC = 0, 1
 BF_PTR_HOST, BF_PTR_DEVICE = 0, 1
 BF_STORE_C32, BF_STORE_FF = 0, 1
 RANK_REC_LEN = 18  # BF_RANK_REC_LEN
@@ -22,7 +23,8 @@ class BuildOpts(C.Structure):
     _fields_ = [("c_tau", f64), ("min_samples", i32), ("adaptive", i32), ("seed", u64),
                 ("rank_mode", i32), ("keep_mixed", i32), ("surrogate_weights", P(C.c_float)),
                 ("surrogate_nweights", i64), ("surrogate_margin", f64),
-                ("factor_storage", i32)]
+                ("factor_storage", i32), ("estimator", i32), ("geo_rmin", i32),
+                ("geo_c", f64), ("geo_ceps", f64)]
 
 
 class TrainOpts(C.Structure):

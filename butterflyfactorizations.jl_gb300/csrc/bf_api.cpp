@@ -110,6 +110,10 @@ void bf_build_opts_default(bf_build_opts* o) {
   o->keep_mixed = 1;
   o->surrogate_margin = 0.15;
   o->factor_storage = BF_STORE_C32;
+  o->estimator = BF_EST_BUTTERFLY;
+  o->geo_rmin = 3;
+  o->geo_c = 1.5;
+  o->geo_ceps = 1.5;
 }
 
 void bf_train_opts_default(bf_train_opts* o) {

@@ -187,12 +187,31 @@ class Builder {
     t.n_cols = n_cols;
     t.key = task_key(opts_.seed, f, stage, obs_node, src_node);
     t.eps = st.eps;
-    t.n_est = std::min(std::max(st.n_est, opts_.min_samples), t.n_obs);
+    const int32_t est = opts_.estimator == BF_EST_GEOMETRIC ? geometric_rank(obs_node, src_node, st.eps)
+                                                            : st.n_est;
+    t.n_est = std::min(std::max(est, opts_.min_samples), t.n_obs);
     t.rows0 = t.rows = t.n_est;
     t.seeded = t.fell_back = 0;
     t.t_off = -1;
     return t;
   }
+  // GeometricRankEstimator (rankestimation.jl:13-25 with the tree method of
+  // ext/BFH2Trees/h2rankest.jl:8-38): x1 = (k a_s a_o / max(d, 1e-4))^2 from the
+  // node radii and the center distance, x2 = log(1/eps),
+  // max(ceil(C x1 + Ceps x2), Rmin)
+  int32_t geometric_rank(int64_t obs_node, int64_t src_node, double eps) const {
+    double d2 = 0;
+    for (int a = 0; a < 3; ++a) {
+      const double d = ts_.center[3 * src_node + a] - to_.center[3 * obs_node + a];
+      d2 += d * d;
+    }
+    const double d = std::max(std::sqrt(d2), 1e-4);
+    const double g = k_ * (ts_.radius(src_node) * to_.radius(obs_node)) / d;
+    const double r = std::ceil(opts_.geo_c * (g * g) + opts_.geo_ceps * std::log(1.0 / eps));
+    const double cap = 1e9;  // keeps the count in int range; rows are capped by n_obs anyway
+    return std::max((int32_t)std::min(r, cap), opts_.geo_rmin);
+  }
+
   // surrogate-seeded sample counts for one round of compressions (GPU inference)
   int seed_rows(std::vector<HTask>& tasks);
 
@@ -1108,6 +1127,16 @@ extern "C" int bf_build(bf_ctx_t ctx, const double* obs_xyz, int64_t n_obs,
     else
       bf_build_opts_default(&o);
     if (o.min_samples < 1) o.min_samples = 1;
+    if (o.estimator != BF_EST_BUTTERFLY && o.estimator != BF_EST_GEOMETRIC) {
+      set_error("bf_build: unknown rank estimator %d", o.estimator);
+      return BF_EINVAL;
+    }
+    if (o.estimator == BF_EST_GEOMETRIC &&
+        (!(o.geo_c >= 0.0) || !(o.geo_ceps >= 0.0) || !std::isfinite(o.geo_c) ||
+         !std::isfinite(o.geo_ceps) || o.geo_rmin < 1)) {
+      set_error("bf_build: geometric estimator needs finite C, Ceps >= 0 and Rmin >= 1");
+      return BF_EINVAL;
+    }
     auto* h = new bf_operator;
     int s = build_operator(&ctx->c, obs_xyz, n_obs, src_xyz, n_src, obs_tree->t, src_tree->t,
                            far_obs, far_src, n_far, k, tol, o, h->op);

@@ -10,6 +10,7 @@ module BFGPU
 
 using LinearAlgebra
 using LinearMaps
+import ButterflyFactorizations
 using ButterflyFactorizations: cluster_root, cluster_children, cluster_values, cluster_center,
                                cluster_radius, cluster_testtree, cluster_trialtree
 import ButterflyFactorizations: PetrovGalerkinBF, assemble_BF, recompress_BF
@@ -149,6 +150,10 @@ struct BuildOpts
     surrogate_nweights::Int64
     surrogate_margin::Float64
     factor_storage::Int32
+    estimator::Int32      # 0: ButterflyRankEstimator(c_tau), 1: GeometricRankEstimator
+    geo_rmin::Int32
+    geo_c::Float64
+    geo_ceps::Float64
 end
 
 const BF_STORE_C32 = Int32(0)
@@ -236,10 +241,17 @@ end
 
 function _build(ctx::Context, X::AbstractMatrix{Float64}, Y::AbstractMatrix{Float64},
                 to::GPUTree, ts::GPUTree, fo::Vector{Int64}, fs::Vector{Int64}, k, tol;
-                c_tau, adaptive, seed, min_samples, storage)
+                c_tau, adaptive, seed, min_samples, storage, rankestimator=nothing)
     size(X, 1) == 3 && size(Y, 1) == 3 || error("point sets are 3 x N matrices")
+    # the reference's estimator objects (rankestimation.jl:13-41) map onto the options
+    est, gc, ge, gr = Int32(0), 1.5, 1.5, Int32(3)
+    if rankestimator isa ButterflyFactorizations.GeometricRankEstimator
+        est, gc, ge, gr = Int32(1), rankestimator.C, rankestimator.Cε, Int32(rankestimator.Rmin)
+    elseif rankestimator isa ButterflyFactorizations.ButterflyRankEstimator
+        c_tau = rankestimator.Cε
+    end
     o = Ref(BuildOpts(c_tau, min_samples, adaptive, seed, 0, 1, C_NULL, 0, 0.15,
-                      storage === :ff ? BF_STORE_FF : BF_STORE_C32))
+                      storage === :ff ? BF_STORE_FF : BF_STORE_C32, est, gr, gc, ge))
     x = Matrix{Float64}(X); y = Matrix{Float64}(Y)
     h = Ref{Ptr{Cvoid}}(C_NULL)
     check(ccall((:bf_build, lib), Cint,
@@ -288,12 +300,13 @@ function PetrovGalerkinBF(::HelmholtzPoints, X::AbstractMatrix{Float64},
                           Y::AbstractMatrix{Float64}, tree, k::Float64; tol=1e-3, alpha=1.0,
                           Ctau=2.9592, minbflvl=3, leafcomp=true, leafimbalance=true,
                           unbalancedints=false, adaptive=true, farfieldonly=false, seed=0,
-                          min_samples=10, storage=:c32, ctx::Context=Context(0))
+                          min_samples=10, storage=:c32, rankestimator=nothing,
+                          ctx::Context=Context(0))
     to = GPUTree(cluster_testtree(tree), size(X, 2))
     ts = GPUTree(cluster_trialtree(tree), size(Y, 2))
     fo, fs, _ = nearandfar_gpu(to, ts; alpha, minbflvl, leafcomp, leafimbalance, unbalancedints)
     A = _build(ctx, X, Y, to, ts, fo, fs, k, tol; c_tau=Ctau, adaptive=Int32(adaptive),
-               seed=UInt64(seed), min_samples=Int32(min_samples), storage)
+               seed=UInt64(seed), min_samples=Int32(min_samples), storage, rankestimator)
     if !farfieldonly
         no, ns = near_pairs_gpu(to, ts; alpha, minbflvl, leafcomp, leafimbalance, unbalancedints)
         x = Matrix{Float64}(X); y = Matrix{Float64}(Y)
@@ -362,13 +375,13 @@ reference's 1-based node ids), compressed on the GPU.
 function assemble_BF(::HelmholtzPoints, blktree, no::Int, ns::Int, k::Float64, tau::Float64;
                      X::AbstractMatrix{Float64}, Y::AbstractMatrix{Float64}, Ctau=4.0,
                      adaptive=true, seed=0, min_samples=10, storage=:c32,
-                     ctx::Context=Context(0))
+                     rankestimator=nothing, ctx::Context=Context(0))
     to = GPUTree(cluster_testtree(blktree), size(X, 2))
     ts = GPUTree(cluster_trialtree(blktree), size(Y, 2))
     fo = Int64[findfirst(==(no), to.order) - 1]
     fs = Int64[findfirst(==(ns), ts.order) - 1]
     return _build(ctx, X, Y, to, ts, fo, fs, k, tau; c_tau=Ctau, adaptive=Int32(adaptive),
-                  seed=UInt64(seed), min_samples=Int32(min_samples), storage)
+                  seed=UInt64(seed), min_samples=Int32(min_samples), storage, rankestimator)
 end
 
 """

@@ -157,7 +157,19 @@ typedef struct {
                               float-float entries, 16 B, the FP64-width layout
                               that ComplexF64 factors (the reference's acctype,
                               bfassembly.jl:61) import into                     */
+  int32_t estimator;     /* rank estimator of the sample counts:
+                            BF_EST_BUTTERFLY (default): ButterflyRankEstimator(c_tau),
+                            max(ceil(c_tau log(1/eps)), 10), rankestimation.jl:93-98;
+                            BF_EST_GEOMETRIC: GeometricRankEstimator(geo_c, geo_ceps;
+                            Rmin=geo_rmin), max(ceil(C (k a_s a_o / d)^2 + Ceps log(1/eps)),
+                            Rmin) with the node radii a and the center distance d
+                            (rankestimation.jl:13-25, ext/BFH2Trees/h2rankest.jl:8-38)   */
+  int32_t geo_rmin;      /* default 3                                              */
+  double geo_c;          /* default 1.5                                            */
+  double geo_ceps;       /* default 1.5                                            */
 } bf_build_opts;
+
+enum { BF_EST_BUTTERFLY = 0, BF_EST_GEOMETRIC = 1 };
 
 /* ---- factor storage of GPU-built operators (bf_build_opts.factor_storage) ---- */
 enum {

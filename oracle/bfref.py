@@ -343,6 +343,20 @@ def estimate_rank_butterfly(eps: float, c_tau: float, rmin: int = 10) -> int:
     return max(int(math.ceil(c_tau * math.log(1.0 / eps))), rmin)
 
 
+def estimate_rank_3d(k: float, tree_s: Tree, tree_o: Tree, snode: int, onode: int, eps: float,
+                     C: float = 1.5, Ceps: float = 1.5, Rmin: int = 3) -> int:
+    """``GeometricRankEstimator`` (``rankestimation.jl:13-25``) with the tree method of
+    ``ext/BFH2Trees/h2rankest.jl:8-38``: x1 = (k a_s a_o / max(d, 1e-4))^2 from the node
+    radii and the center distance, x2 = log(1/eps), max(ceil(C x1 + Ceps x2), Rmin)."""
+    d2 = 0.0
+    for a in range(3):
+        dd = float(tree_s.center[snode, a]) - float(tree_o.center[onode, a])
+        d2 += dd * dd
+    d = max(math.sqrt(d2), 1e-4)
+    g = k * (tree_s.radius(snode) * tree_o.radius(onode)) / d
+    return max(int(math.ceil(C * (g * g) + Ceps * math.log(1.0 / eps))), Rmin)
+
+
 def pqr_rank(R: np.ndarray, rtol: float) -> int:
     """Rank of a column-pivoted QR truncated at |R_ii| <= rtol |R_00|.
 
@@ -468,7 +482,7 @@ class BF:
 
 def assemble_bf(kern, tree_o: Tree, tree_s: Tree, no: int, ns: int, k: float, tau: float,
                 c_tau: float = 4.0, adaptive: bool = True, seed: int = 0, bf_id: int = 0,
-                min_samples: int = 10, log: list | None = None) -> BF:
+                min_samples: int = 10, log: list | None = None, geometric=None) -> BF:
     """``assemble_BF`` (``src/ButterflyFactorization/bfassembly.jl:48-200``).
 
     ``c_tau`` is the ButterflyRankEstimator constant (default ``Ctau=4.0``,
@@ -485,7 +499,11 @@ def assemble_bf(kern, tree_o: Tree, tree_s: Tree, no: int, ns: int, k: float, ta
     K = {}
 
     def comp(src, obs, stage, onode, snode):
-        return partial_qr(kern, src, obs, n_est, eps, adaptive,
+        # geometric = (C, Ceps, Rmin): the GeometricRankEstimator at every call site
+        # (the reference calls rankestimator(k, trialT, testT, Snode, Onode, tau_scaled))
+        est = n_est if geometric is None else estimate_rank_3d(k, tree_s, tree_o, snode, onode,
+                                                               eps, *geometric)
+        return partial_qr(kern, src, obs, est, eps, adaptive,
                           task_key(seed, bf_id, stage, onode, snode), min_samples, log)
 
     # Q stage (bfassembly.jl:82-102)

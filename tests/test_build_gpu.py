@@ -116,3 +116,32 @@ def test_build_is_deterministic(ctx):
     x = G.complex_gaussian(n, 5)
     assert np.array_equal(a @ x, b @ x)
     assert np.array_equal(a.adjoint() @ x, b.adjoint() @ x)
+
+
+def test_geometric_rank_estimator(c1, ctx):
+    """GeometricRankEstimator(1.5, 1.5; Rmin=3) (rankestimation.jl:13-25,
+    ext/BFH2Trees/h2rankest.jl:8-38): every compression's initial sample count is the
+    oracle's estimate for its node pair, and the operator meets the dense criterion."""
+    est = bfgpu.GeometricRankEstimator(1.5, 1.5, 3)
+    op = bfgpu.assemble_BF(c1["obs"], c1["src"], c1["to"], c1["ts"], 0, 0, c1["k"], TOL,
+                           c_tau=4.0, seed=3, ctx=ctx, rank_estimator=est)
+    A = c1["kern"](np.arange(4096), np.arange(4096))
+    x = G.complex_gaussian(4096, 9)
+    assert relerr(op @ x, A @ x) < 10 * TOL
+    ot = O.build_tree(c1["obs"], max_depth=4)
+    os_ = O.build_tree(c1["src"], max_depth=4)
+    L = max(len(O.traverseandpad(ot, 0)), len(O.traverseandpad(os_, 0)))
+    eps = TOL / L
+    log = op.rank_log()
+    rows0 = log[:, 6].astype(np.int64)
+    want = np.array([min(max(O.estimate_rank_3d(c1["k"], os_, ot, int(r[3]), int(r[2]), eps,
+                                                1.5, 1.5, 3), 10), int(r[4])) for r in log])
+    assert np.array_equal(rows0, want)
+    # the estimator changes the samples: not the ButterflyRankEstimator's single count
+    assert len(np.unique(rows0)) > 1
+    bf = O.assemble_bf(c1["kern"], ot, os_, 0, 0, c1["k"], TOL, c_tau=4.0, seed=3,
+                       geometric=(1.5, 1.5, 3))
+    gbf = export_to_oracle(op.export_blocks(), ot, os_)[0]
+    rq = np.array([b.data.shape[0] for b in gbf.Q])
+    ro = np.array([b.data.shape[0] for b in bf.Q])
+    assert np.mean(np.abs(rq - ro) <= 1) > 0.95
