@@ -84,8 +84,11 @@ __device__ __forceinline__ void warp_tall(const DTask& t, int r0, const FT* __re
   bool act[TALL_RPL];
 #pragma unroll
   for (int q = 0; q < TALL_RPL; ++q) act[q] = r0 + lane + 32 * q < M;
-  // columns per batch: 128 bytes of factor loads per lane
-  constexpr int CPI = (sizeof(FT) == 8 ? 16 : 8) / TALL_RPL;
+  // columns per batch: 128 bytes of factor loads per lane; with complex FP32
+  // factors and several right-hand sides, 32 bytes (the NR accumulators need the
+  // registers: 80 instead of 128 per thread, three CTAs per SM instead of two;
+  // measured 1.16x on 262,144-point operators with 8 right-hand sides)
+  constexpr int CPI = (sizeof(FT) == 8 ? (NR > 1 ? 4 : 16) : 8) / TALL_RPL;
   for (int cb = 0; cb < n; cb += XB) {
     const int nb = min(XB, n - cb);  // warp-uniform
     const FT* __restrict__ ap = A + t.a_off + (size_t)cb * M + r0 + lane;
