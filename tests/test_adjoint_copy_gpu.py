@@ -75,3 +75,37 @@ def test_refusals(ctx):
                                   farfieldonly=False, ctx=ctx)
     with pytest.raises(bfgpu.BFError, match="near field"):
         full.adjoint_copy()
+
+
+def test_copy_of_recompressed_and_persisted(ctx, tmp_path):
+    # the features compose: recompress, materialise the adjoint, save, load
+    obs, src = G.plane_pair(4096, seed=1)
+    k = 2 * math.pi / 0.125
+    to, ts = bfgpu.Tree.build(obs, max_depth=4), bfgpu.Tree.build(src, max_depth=4)
+    op = bfgpu.assemble_BF(obs, src, to, ts, 0, 0, k, 1e-4, c_tau=4.0, seed=3, ctx=ctx)
+    rop = op.recompress(1e-2)
+    c = rop.adjoint_copy()
+    path = str(tmp_path / "c.bfop")
+    c.save(path)
+    back = bfgpu.load_operator(path, ctx)
+    X = G.complex_gaussian(4096, 33, nrhs=2)
+    assert np.array_equal(back.matvec(X), c.matvec(X))
+    assert relerr(back.matvec(X), rop.adjoint().matvec(X)) <= PARITY
+    assert relerr(back.adjoint().matvec(X), op.matvec(X)) < 10 * 1e-2
+
+
+def test_recompression_at_extreme_tolerances(ctx):
+    obs, src = G.plane_pair(4096, seed=1)
+    k = 2 * math.pi / 0.125
+    to, ts = bfgpu.Tree.build(obs, max_depth=4), bfgpu.Tree.build(src, max_depth=4)
+    op = bfgpu.assemble_BF(obs, src, to, ts, 0, 0, k, 1e-4, c_tau=4.0, seed=3, ctx=ctx)
+    X = G.complex_gaussian(4096, 34)
+    y = op.matvec(X)
+    # far above the build tolerance: ranks collapse, the product is still an operator
+    coarse = op.recompress(0.5)
+    assert coarse.stats()["factor_entries"] < op.stats()["factor_entries"]
+    assert np.all(np.isfinite(coarse.matvec(X)))
+    # far below it: little to take, the product within FP32 arithmetic of the input
+    fine = op.recompress(1e-7)
+    assert fine.stats()["factor_entries"] <= op.stats()["factor_entries"]
+    assert relerr(fine.matvec(X), y) < 1e-4
