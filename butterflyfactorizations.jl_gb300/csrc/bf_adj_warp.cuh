@@ -33,7 +33,11 @@ __device__ __forceinline__ float4 vin(const DTask& t, const int32_t* __restrict_
   return t.rbase >= 0 ? ws[((long long)t.rbase + r) * S] : ws[(long long)rmap[r] * S];
 }
 
-__device__ __forceinline__ int rg_of(int M) { return M <= 8 ? 2 : (M <= 32 ? 4 : 8); }
+// row groups per column: 4 up to 64 rows (a lane walks up to 16 rows of a column
+// and the partial sums meet in 2 shuffle steps; 8 groups for M in 33..64 spent a
+// quarter of the arithmetic on the 3-step reduction: 6% slower adjoints with
+// complex FP32 factors at 262,144 points)
+__host__ __device__ __forceinline__ int rg_of(int M) { return M <= 8 ? 2 : (M <= 64 ? 4 : 8); }
 
 constexpr int ADJ_VS = 128;  // staged input entries per warp
 
@@ -137,7 +141,7 @@ __host__ __device__ __forceinline__ int adj_cpl(int n, int CG) {
 // Column passes of a task for the warp routine below (per_pass columns
 // each): the batch splits wide tasks into work items by pass.
 __host__ __device__ __forceinline__ int adj_passes(int M, int n) {
-  const int CG = 32 / (M <= 8 ? 2 : (M <= 32 ? 4 : 8));
+  const int CG = 32 / rg_of(M);
   const int per_pass = CG * adj_cpl(n, CG);
   return (n + per_pass - 1) / per_pass;
 }
