@@ -445,10 +445,14 @@ def run_rows(args, rank, world, local):
         if with_cpu:
             bfs = O.from_blocks(op.export_blocks(), O.CsrTree(*to.values_csr()),
                                 O.CsrTree(*ts.values_csr()))
+            # CPU baseline and checker: the oracle's restatement of recompress_BF on the
+            # same exported blocks (outside any GPU timing)
             t0 = time.perf_counter()
             rbs = [O.recompress_bf(bf, 1e-2) for bf in bfs]
-            r["oracle_cpu_s"] = time.perf_counter() - t0
-            r["oracle_cpu_threads"] = 1
+            r["cpu_baseline"] = {"value": time.perf_counter() - t0, "unit": "s", "cores": 1,
+                                 "kind": "port",
+                                 "sample": "the whole far block: recompress_BF restated in "
+                                           "NumPy/SciPy (LAPACK pivoted QR)"}
             r["factor_entries"]["oracle"] = int(sum(O.factor_entries(b) for b in rbs))
             yo = O.apply_far(rbs, xs, npl)
             r["rel_diff_vs_oracle"] = float(np.linalg.norm(rop.matvec(xs) - yo) / np.linalg.norm(yo))
