@@ -219,14 +219,19 @@ function GPUTree(tree, npoints::Integer)
 end
 
 """
-    nearandfar_gpu(testtree, trialtree; alpha, minbflvl, leafcomp, leafimbalance)
+    nearandfar_gpu(testtree, trialtree; alpha, minbflvl, leafcomp, leafimbalance,
+                   unbalancedints, ctx=nothing)
 
 Far pairs (library node ids, 0-based) and the near-pair count: the dual-tree
 traversal of src/Matrixassembly/intlists.jl:30-217 with the AABB isFarFunctor
-of ext/BFH2Trees/h2admissible.jl:11-45.
+of ext/BFH2Trees/h2admissible.jl:11-45.  With `ctx` a Context the traversal
+runs on that GPU (bf_nearandfar_gpu) and gives the same pairs in the same
+order; without it, on the host (bf_nearandfar).
 """
 function nearandfar_gpu(to::GPUTree, ts::GPUTree; alpha=1.0, minbflvl=3, leafcomp=true,
-                        leafimbalance=true, unbalancedints=false)
+                        leafimbalance=true, unbalancedints=false, ctx=nothing)
+    ctx === nothing || return _nearandfar_device(ctx, to, ts, alpha, minbflvl, leafcomp,
+                                                 leafimbalance, unbalancedints)[1:3]
     nf = Ref{Int64}(0); nn = Ref{Int64}(0)
     args(fo, fs, cap) = ccall((:bf_nearandfar, lib), Cint,
                               (Ptr{Cvoid}, Ptr{Cvoid}, Float64, Int32, Int32, Int32, Int32,
@@ -237,6 +242,24 @@ function nearandfar_gpu(to::GPUTree, ts::GPUTree; alpha=1.0, minbflvl=3, leafcom
     fo = zeros(Int64, max(nf[], 1)); fs = zeros(Int64, max(nf[], 1))
     check(args(fo, fs, length(fo)), "bf_nearandfar")
     return fo[1:nf[]], fs[1:nf[]], Int(nn[])
+end
+
+# one device traversal: far pairs, near-pair count, near pairs
+function _nearandfar_device(ctx::Context, to::GPUTree, ts::GPUTree, alpha, minbflvl, leafcomp,
+                            leafimbalance, unbalancedints)
+    nf = Ref{Int64}(0); nn = Ref{Int64}(0)
+    args(fo, fs, fcap, no, ns, ncap) =
+        ccall((:bf_nearandfar_gpu, lib), Cint,
+              (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Float64, Int32, Int32, Int32, Int32,
+               Ptr{Int64}, Ptr{Int64}, Int64, Ptr{Int64}, Ptr{Int64}, Int64,
+               Ref{Int64}, Ref{Int64}),
+              ctx.h, to.h, ts.h, alpha, minbflvl, leafcomp, leafimbalance, unbalancedints,
+              fo, fs, fcap, no, ns, ncap, nf, nn)
+    check(args(C_NULL, C_NULL, 0, C_NULL, C_NULL, 0), "bf_nearandfar_gpu")
+    fo = zeros(Int64, max(nf[], 1)); fs = zeros(Int64, max(nf[], 1))
+    no = zeros(Int64, max(nn[], 1)); ns = zeros(Int64, max(nn[], 1))
+    check(args(fo, fs, length(fo), no, ns, length(no)), "bf_nearandfar_gpu")
+    return fo[1:nf[]], fs[1:nf[]], Int(nn[]), no[1:nn[]], ns[1:nn[]]
 end
 
 function _build(ctx::Context, X::AbstractMatrix{Float64}, Y::AbstractMatrix{Float64},
@@ -264,12 +287,16 @@ function _build(ctx::Context, X::AbstractMatrix{Float64}, Y::AbstractMatrix{Floa
 end
 
 """
-    near_pairs_gpu(testtree, trialtree; alpha, minbflvl, leafcomp, leafimbalance)
+    near_pairs_gpu(testtree, trialtree; alpha, minbflvl, leafcomp, leafimbalance,
+                   unbalancedints, ctx=nothing)
 
-Near pairs (library node ids, 0-based) of the same traversal as nearandfar_gpu.
+Near pairs (library node ids, 0-based) of the same traversal as nearandfar_gpu,
+on the GPU of `ctx` when one is given.
 """
 function near_pairs_gpu(to::GPUTree, ts::GPUTree; alpha=1.0, minbflvl=3, leafcomp=true,
-                        leafimbalance=true, unbalancedints=false)
+                        leafimbalance=true, unbalancedints=false, ctx=nothing)
+    ctx === nothing || return _nearandfar_device(ctx, to, ts, alpha, minbflvl, leafcomp,
+                                                 leafimbalance, unbalancedints)[4:5]
     nn = Ref{Int64}(0)
     args(no, ns, cap) = ccall((:bf_near_pairs, lib), Cint,
                               (Ptr{Cvoid}, Ptr{Cvoid}, Float64, Int32, Int32, Int32, Int32,
