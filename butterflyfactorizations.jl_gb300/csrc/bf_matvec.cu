@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(FW_WARPS * 32) fwd_tall_kernel(
   if (item >= n_items) return;
   const int2 it = items[item];
   const DTask t = tasks[it.x];
-  warp_tall<FT>(t, it.y, A, maps, ws, xs[warp]);
+  warp_tall_one<FT>(t, it.y, A, maps, ws, xs[warp]);
 }
 
 template <typename FT>
@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(FW_WARPS * 32) fwd_small_kernel(
   const int ti = blockIdx.x * FW_WARPS + warp;
   if (ti >= n_tasks) return;
   const DTask t = tasks[tlist[ti]];
-  warp_small<FT>(t, A, maps, ws, xs[warp]);
+  warp_small_one<FT>(t, A, maps, ws, xs[warp]);
 }
 
 __global__ void copy_kernel(const int32_t* __restrict__ tlist, int n_tasks,
