@@ -49,14 +49,18 @@ __device__ __forceinline__ void adj_stage(const DTask& t, const int32_t* __restr
 }
 
 // Adds, for this lane, the partial sums of columns c = c0 + cg + CG*u (u < cpl)
-// over rows [r_begin, r_end) whose input entries are staged at vs[r - vbase].
+// over rows [r_begin, r_end) whose input entries are staged at vs[r - vbase],
+// every entry under a guard: the form the batch kernels keep (the unguarded
+// one below takes registers their work-queue loop needs) and the level
+// kernels use with complex FP32 factors.
 // The input entries are gathered once into shared memory (adj_stage), so the
 // row walk waits on the factor loads only, not on a routing-map lookup and a
 // dependent workspace load per row.
 template <bool CONJ, int RG, typename FT>
-__device__ __forceinline__ void adj_accum(const DTask& t, const FT* __restrict__ A,
-                                          const float4* __restrict__ vs, int vbase, int r_begin,
-                                          int r_end, int c0, int cpl, float4 acc[ADJ_CPL]) {
+__device__ __forceinline__ void adj_accum_guarded(const DTask& t, const FT* __restrict__ A,
+                                                  const float4* __restrict__ vs, int vbase,
+                                                  int r_begin, int r_end, int c0, int cpl,
+                                                  float4 acc[ADJ_CPL]) {
   constexpr int CG = 32 / RG;
   const int lane = threadIdx.x & 31;
   const int rg = lane % RG, cg = lane / RG;
@@ -84,6 +88,56 @@ __device__ __forceinline__ void adj_accum(const DTask& t, const FT* __restrict__
   }
 }
 
+// Adds, for this lane, the partial sums of columns c = c0 + cg + CG*u (u < CPL)
+// over rows [r_begin, r_end) whose input entries are staged at vs[r - vbase].
+// The input entries are gathered once into shared memory (adj_stage), so the
+// row walk waits on the factor loads only, not on a routing-map lookup and a
+// dependent workspace load per row.  CPL is a template parameter and a column
+// past the task's end reads column n - 1 instead (in bounds; its sum is never
+// written), so the row walk carries no per-entry guards.
+template <bool CONJ, int RG, int CPL, typename FT>
+__device__ __forceinline__ void adj_accum(const DTask& t, const FT* __restrict__ A,
+                                          const float4* __restrict__ vs, int vbase, int r_begin,
+                                          int r_end, int c0, float4 acc[ADJ_CPL]) {
+  constexpr int CG = 32 / RG;
+  const int lane = threadIdx.x & 31;
+  const int rg = lane % RG, cg = lane / RG;
+  const int M = t.M, n = t.n;
+  const FT* __restrict__ Ab = A + t.a_off;
+  long long coff[CPL];
+#pragma unroll
+  for (int u = 0; u < CPL; ++u) coff[u] = (long long)min(c0 + cg + CG * u, n - 1) * M;
+  // (two row steps per iteration were measured slower: the extra registers
+  // cost more occupancy than the extra loads in flight gained)
+  for (int r = r_begin + rg; r < r_end; r += RG) {
+    const float4 v = vs[r - vbase];
+    FT a[CPL];
+#pragma unroll
+    for (int u = 0; u < CPL; ++u) a[u] = __ldg(Ab + coff[u] + r);
+#pragma unroll
+    for (int u = 0; u < CPL; ++u) {
+      if (CONJ)
+        cdf_mac_conj(acc[u], a[u], v);
+      else
+        cdf_mac(acc[u], a[u], v);
+    }
+  }
+}
+
+template <bool CONJ, int RG, typename FT>
+__device__ __forceinline__ void adj_accum_n(const DTask& t, const FT* __restrict__ A,
+                                            const float4* __restrict__ vs, int vbase,
+                                            int r_begin, int r_end, int c0, int cpl,
+                                            float4 acc[ADJ_CPL]) {
+  static_assert(ADJ_CPL == 4, "one case per column count");
+  switch (cpl) {
+    case 1: adj_accum<CONJ, RG, 1, FT>(t, A, vs, vbase, r_begin, r_end, c0, acc); break;
+    case 2: adj_accum<CONJ, RG, 2, FT>(t, A, vs, vbase, r_begin, r_end, c0, acc); break;
+    case 3: adj_accum<CONJ, RG, 3, FT>(t, A, vs, vbase, r_begin, r_end, c0, acc); break;
+    default: adj_accum<CONJ, RG, 4, FT>(t, A, vs, vbase, r_begin, r_end, c0, acc); break;
+  }
+}
+
 // the RG partial sums of each column meet (every lane of the group holds the total)
 template <int RG>
 __device__ __forceinline__ void adj_reduce(float4 acc[ADJ_CPL], int cpl) {
@@ -96,7 +150,7 @@ __device__ __forceinline__ void adj_reduce(float4 acc[ADJ_CPL], int cpl) {
 
 // rows [r0, r1) of column pass c0 for this warp: already staged (staged =
 // true, at vs[r - r0]) or staged here in chunks of ADJ_VS rows
-template <bool CONJ, int RG, typename FT>
+template <bool CONJ, int RG, typename FT, bool FAST = false>
 __device__ __forceinline__ void adj_rows(const DTask& t, const FT* __restrict__ A,
                                          const int32_t* __restrict__ rmap,
                                          const float4* __restrict__ ws, float4* __restrict__ vs,
@@ -104,15 +158,21 @@ __device__ __forceinline__ void adj_rows(const DTask& t, const FT* __restrict__ 
                                          float4 acc[ADJ_CPL], int S = 1) {
 #pragma unroll
   for (int u = 0; u < ADJ_CPL; ++u) acc[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+  auto walk = [&](int vbase, int rb, int re) {
+    if constexpr (FAST)
+      adj_accum_n<CONJ, RG, FT>(t, A, vs, vbase, rb, re, c0, cpl, acc);
+    else
+      adj_accum_guarded<CONJ, RG, FT>(t, A, vs, vbase, rb, re, c0, cpl, acc);
+  };
   if (staged) {
-    adj_accum<CONJ, RG, FT>(t, A, vs, r0, r0, r1, c0, cpl, acc);
+    walk(r0, r0, r1);
   } else {
     for (int rc = r0; rc < r1; rc += ADJ_VS) {  // chunk starts stay multiples of RG
       const int len = min(ADJ_VS, r1 - rc);
       __syncwarp();
       adj_stage(t, rmap, ws, vs, rc, len, S);
       __syncwarp();
-      adj_accum<CONJ, RG, FT>(t, A, vs, rc, rc, rc + len, c0, cpl, acc);
+      walk(rc, rc, rc + len);
     }
   }
   adj_reduce<RG>(acc, cpl);
@@ -146,7 +206,7 @@ __host__ __device__ __forceinline__ int adj_passes(int M, int n) {
   return (n + per_pass - 1) / per_pass;
 }
 
-template <bool CONJ, int RG, typename FT>
+template <bool CONJ, int RG, typename FT, bool FAST = false>
 __device__ void adj_task_warp(const DTask& t, const FT* __restrict__ A,
                               const int32_t* __restrict__ maps, float4* __restrict__ ws,
                               float4* __restrict__ vs, int pass_begin, int pass_step,
@@ -166,7 +226,7 @@ __device__ void adj_task_warp(const DTask& t, const FT* __restrict__ A,
   }
   float4 acc[ADJ_CPL];
   for (int c0 = pass_begin * per_pass; c0 < t.n; c0 += pass_step * per_pass) {
-    adj_rows<CONJ, RG, FT>(t, A, rmap, ws, vs, staged, 0, t.M, c0, cpl, acc, S);
+    adj_rows<CONJ, RG, FT, FAST>(t, A, rmap, ws, vs, staged, 0, t.M, c0, cpl, acc, S);
     if (rg == 0) {
 #pragma unroll
       for (int u = 0; u < ADJ_CPL; ++u) {
