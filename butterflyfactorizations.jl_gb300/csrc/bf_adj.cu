@@ -16,7 +16,9 @@ namespace {
 // Row walks without per-entry guards (adj_accum) for float-float factors:
 // 17.73 -> 15.69 ms for the adjoint of the 262,144-point sphere operator.
 // With complex FP32 factors they made the Q-level kernel spill and the whole
-// adjoint slower (12.98 -> 13.71 ms), so those keep the guarded walk.
+// adjoint slower (12.98 -> 13.71 ms), so those keep the guarded walk.  The
+// tall kernel's walk takes two row steps per iteration, both steps' loads
+// issued first (80 registers, no spills; its level 3.20 -> 3.11 ms).
 template <typename FT>
 constexpr bool UNGUARDED = sizeof(FT) == sizeof(float4);
 
@@ -86,7 +88,7 @@ __global__ void __launch_bounds__(256) adj_tall_kernel(const int32_t* __restrict
   }
   float4 acc[ADJ_CPL];
   for (int c0 = 0; c0 < t.n; c0 += per_pass) {
-    adj_rows<CONJ, RG, FT, UNGUARDED<FT>>(t, A, rmap, ws, vsm[w], staged, r0, r1, c0, cpl, acc);
+    adj_rows<CONJ, RG, FT, UNGUARDED<FT>, 2>(t, A, rmap, ws, vsm[w], staged, r0, r1, c0, cpl, acc);
     if (rg == 0) {
 #pragma unroll
       for (int u = 0; u < ADJ_CPL; ++u)

@@ -95,7 +95,7 @@ __device__ __forceinline__ void adj_accum_guarded(const DTask& t, const FT* __re
 // dependent workspace load per row.  CPL is a template parameter and a column
 // past the task's end reads column n - 1 instead (in bounds; its sum is never
 // written), so the row walk carries no per-entry guards.
-template <bool CONJ, int RG, int CPL, typename FT>
+template <bool CONJ, int RG, int CPL, typename FT, int U = 1>
 __device__ __forceinline__ void adj_accum(const DTask& t, const FT* __restrict__ A,
                                           const float4* __restrict__ vs, int vbase, int r_begin,
                                           int r_end, int c0, float4 acc[ADJ_CPL]) {
@@ -109,7 +109,34 @@ __device__ __forceinline__ void adj_accum(const DTask& t, const FT* __restrict__
   for (int u = 0; u < CPL; ++u) coff[u] = (long long)min(c0 + cg + CG * u, n - 1) * M;
   // (two row steps per iteration were measured slower: the extra registers
   // cost more occupancy than the extra loads in flight gained)
-  for (int r = r_begin + rg; r < r_end; r += RG) {
+  int r = r_begin + rg;
+  if constexpr (U == 2) {
+    // two row steps per iteration, both steps' loads issued first
+    for (; r + RG < r_end; r += 2 * RG) {
+      const float4 v0 = vs[r - vbase], v1 = vs[r + RG - vbase];
+      FT a0[CPL], a1[CPL];
+#pragma unroll
+      for (int u = 0; u < CPL; ++u) {
+        a0[u] = __ldg(Ab + coff[u] + r);
+        a1[u] = __ldg(Ab + coff[u] + r + RG);
+      }
+#pragma unroll
+      for (int u = 0; u < CPL; ++u) {
+        if (CONJ)
+          cdf_mac_conj(acc[u], a0[u], v0);
+        else
+          cdf_mac(acc[u], a0[u], v0);
+      }
+#pragma unroll
+      for (int u = 0; u < CPL; ++u) {
+        if (CONJ)
+          cdf_mac_conj(acc[u], a1[u], v1);
+        else
+          cdf_mac(acc[u], a1[u], v1);
+      }
+    }
+  }
+  for (; r < r_end; r += RG) {
     const float4 v = vs[r - vbase];
     FT a[CPL];
 #pragma unroll
@@ -124,17 +151,17 @@ __device__ __forceinline__ void adj_accum(const DTask& t, const FT* __restrict__
   }
 }
 
-template <bool CONJ, int RG, typename FT>
+template <bool CONJ, int RG, typename FT, int U = 1>
 __device__ __forceinline__ void adj_accum_n(const DTask& t, const FT* __restrict__ A,
                                             const float4* __restrict__ vs, int vbase,
                                             int r_begin, int r_end, int c0, int cpl,
                                             float4 acc[ADJ_CPL]) {
   static_assert(ADJ_CPL == 4, "one case per column count");
   switch (cpl) {
-    case 1: adj_accum<CONJ, RG, 1, FT>(t, A, vs, vbase, r_begin, r_end, c0, acc); break;
-    case 2: adj_accum<CONJ, RG, 2, FT>(t, A, vs, vbase, r_begin, r_end, c0, acc); break;
-    case 3: adj_accum<CONJ, RG, 3, FT>(t, A, vs, vbase, r_begin, r_end, c0, acc); break;
-    default: adj_accum<CONJ, RG, 4, FT>(t, A, vs, vbase, r_begin, r_end, c0, acc); break;
+    case 1: adj_accum<CONJ, RG, 1, FT, U>(t, A, vs, vbase, r_begin, r_end, c0, acc); break;
+    case 2: adj_accum<CONJ, RG, 2, FT, U>(t, A, vs, vbase, r_begin, r_end, c0, acc); break;
+    case 3: adj_accum<CONJ, RG, 3, FT, U>(t, A, vs, vbase, r_begin, r_end, c0, acc); break;
+    default: adj_accum<CONJ, RG, 4, FT, U>(t, A, vs, vbase, r_begin, r_end, c0, acc); break;
   }
 }
 
@@ -150,7 +177,7 @@ __device__ __forceinline__ void adj_reduce(float4 acc[ADJ_CPL], int cpl) {
 
 // rows [r0, r1) of column pass c0 for this warp: already staged (staged =
 // true, at vs[r - r0]) or staged here in chunks of ADJ_VS rows
-template <bool CONJ, int RG, typename FT, bool FAST = false>
+template <bool CONJ, int RG, typename FT, bool FAST = false, int U = 1>
 __device__ __forceinline__ void adj_rows(const DTask& t, const FT* __restrict__ A,
                                          const int32_t* __restrict__ rmap,
                                          const float4* __restrict__ ws, float4* __restrict__ vs,
@@ -160,7 +187,7 @@ __device__ __forceinline__ void adj_rows(const DTask& t, const FT* __restrict__ 
   for (int u = 0; u < ADJ_CPL; ++u) acc[u] = make_float4(0.f, 0.f, 0.f, 0.f);
   auto walk = [&](int vbase, int rb, int re) {
     if constexpr (FAST)
-      adj_accum_n<CONJ, RG, FT>(t, A, vs, vbase, rb, re, c0, cpl, acc);
+      adj_accum_n<CONJ, RG, FT, U>(t, A, vs, vbase, rb, re, c0, cpl, acc);
     else
       adj_accum_guarded<CONJ, RG, FT>(t, A, vs, vbase, rb, re, c0, cpl, acc);
   };
