@@ -84,7 +84,7 @@ int bf_ctx_create(int device, bf_ctx_t* out) {
     return BF_ECUDA;
   }
   if (h->c.prop.major < 10) {
-    set_error("bf_ctx_create: device %d is sm_%d%d; this build targets sm_103a", device,
+    set_error("bf_ctx_create: device %d is sm_%d%d; the library is compiled for sm_103a", device,
               h->c.prop.major, h->c.prop.minor);
     delete h;
     return BF_ECUDA;
