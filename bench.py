@@ -85,6 +85,8 @@ def parse():
     ap.add_argument("--ncu-case", action="store_true",
                     help="no timing: build, then 2 plain forward matvecs and 2 mixed forward "
                          "128-RHS chunks (a short, predictable launch sequence for ncu)")
+    ap.add_argument("--ncu-adjoint", action="store_true",
+                    help="with --ncu-case: the plain matvecs through the adjoint view")
     return ap.parse_args()
 
 
@@ -478,17 +480,21 @@ def run_ncu_case(args, local):
         return
     w = build_workload(args.workload, local, args.storage)
     op, n = w["op"], w["n"]
+    view = op.adjoint() if args.ncu_adjoint else op
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     sp = stream.cuda_stream
     xd = torch.from_numpy(w["x"]).cuda()
     yd = torch.zeros_like(xd)
     for _ in range(2):
-        op.matvec_ptr(xd.data_ptr(), n, yd.data_ptr(), n, ptr_mode=bfgpu.BF_PTR_DEVICE, stream=sp)
+        view.matvec_ptr(xd.data_ptr(), n, yd.data_ptr(), n, ptr_mode=bfgpu.BF_PTR_DEVICE,
+                        stream=sp)
     torch.cuda.synchronize()
+    view.check(sp)
     out = {"ncu_case": args.workload, "levels": op.stats()["n_stages"],
+           "direction": "adjoint" if args.ncu_adjoint else "forward",
            # algorithmic bytes per level (its launches come after the two matvecs)
-           "stage_bytes": [int(v) for v in op.profile(nrep=1)[1]]}
+           "stage_bytes": [int(v) for v in view.profile(nrep=1)[1]]}
     if not args.no_mixed:
         op.mixed_info()
         X = np.ascontiguousarray(G.complex_gaussian(n, 12, nrhs=128).T)
