@@ -61,16 +61,18 @@ __global__ void __launch_bounds__(256) adj_wide_kernel(const int32_t* __restrict
 
 // CTA per tall task (M > 128): the 8 warps split the rows; per column pass the
 // warp partials meet in shared memory.
-template <bool CONJ, typename FT>
-__global__ void __launch_bounds__(256) adj_tall_kernel(const int32_t* __restrict__ tlist,
-                                                       const DTask* __restrict__ tasks,
-                                                       const FT* __restrict__ A,
-                                                       const int32_t* __restrict__ maps,
-                                                       float4* __restrict__ ws) {
-  constexpr int RG = 8, CG = 4;
-  __shared__ float4 red[8][CG * ADJ_CPL];
-  __shared__ float4 vsm[8][ADJ_VS];
-  const DTask t = tasks[tlist[blockIdx.x]];
+// One CTA per task with more than ADJ_TALL_M rows: the 8 warps split the rows
+// (in multiples of RG), each warp walks its rows for RG row groups x CG = 32/RG
+// column groups, and the warps' column sums meet in shared memory.  A task of
+// more than 16 columns takes RG = 4 (one column pass up to 32 columns) instead
+// of RG = 8 (two passes, each staging the rows' inputs again).
+template <bool CONJ, typename FT, int RG>
+__device__ __forceinline__ void adj_tall_task(const DTask& t, const FT* __restrict__ A,
+                                              const int32_t* __restrict__ maps,
+                                              float4* __restrict__ ws, float4 (*red)[32],
+                                              float4 (*vsm)[ADJ_VS]) {
+  constexpr int CG = 32 / RG;
+  static_assert(CG * ADJ_CPL <= 32, "reduction buffer");
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int rg = lane % RG, cg = lane / RG;
   const int32_t* __restrict__ rmap = maps + t.rmap_off;
@@ -105,6 +107,29 @@ __global__ void __launch_bounds__(256) adj_tall_kernel(const int32_t* __restrict
     }
     __syncthreads();
   }
+}
+
+// float-float factors: at least 3 CTAs per SM, which lets the walk keep its
+// 80 registers (left to itself the compiler chose 64 and spilled, 2.87 against
+// 2.26 ms for the Q level's adjoint at 262,144 points); complex FP32 factors
+// do better with the compiler's own choice (0: no minimum; 60 registers, 1.99
+// against 2.34 ms with the minimum of 3)
+template <typename FT>
+constexpr int ADJ_TALL_MINB = sizeof(FT) == sizeof(float4) ? 3 : 0;
+
+template <bool CONJ, typename FT>
+__global__ void __launch_bounds__(256, ADJ_TALL_MINB<FT>) adj_tall_kernel(const int32_t* __restrict__ tlist,
+                                                       const DTask* __restrict__ tasks,
+                                                       const FT* __restrict__ A,
+                                                       const int32_t* __restrict__ maps,
+                                                       float4* __restrict__ ws) {
+  __shared__ float4 red[8][32];
+  __shared__ float4 vsm[8][ADJ_VS];
+  const DTask t = tasks[tlist[blockIdx.x]];
+  if (t.n > 16)  // block-uniform
+    adj_tall_task<CONJ, FT, 4>(t, A, maps, ws, red, vsm);
+  else
+    adj_tall_task<CONJ, FT, 8>(t, A, maps, ws, red, vsm);
 }
 
 }  // namespace
