@@ -181,6 +181,8 @@ int validate_near(const Operator& op) {
         continue;
       }
       if (v < (adj ? N.n_fwd : 0) || v >= (adj ? nt : N.n_fwd)) return bad("list entry");
+      // the small-task kernel walks the binary digits of M up to 32
+      if (!tall && (N.tasks[v].M < 1 || N.tasks[v].M > 32)) return bad("small task rows");
     }
   }
   return BF_OK;
