@@ -107,8 +107,9 @@ __device__ __forceinline__ void adj_accum(const DTask& t, const FT* __restrict__
   long long coff[CPL];
 #pragma unroll
   for (int u = 0; u < CPL; ++u) coff[u] = (long long)min(c0 + cg + CG * u, n - 1) * M;
-  // (two row steps per iteration were measured slower: the extra registers
-  // cost more occupancy than the extra loads in flight gained)
+  // U = 2: two row steps per iteration.  That pays in the tall kernel (long
+  // row walks, 80 registers at 3 CTAs per SM); in the warp kernels the extra
+  // registers cost more occupancy than the extra loads in flight gained.
   int r = r_begin + rg;
   if constexpr (U == 2) {
     // two row steps per iteration, both steps' loads issued first
