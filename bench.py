@@ -755,8 +755,8 @@ def run_mixed(args, w, stream, world):
 # run).  Traffic grows with the algorithmic bytes (every factor entry and slot
 # is moved once), so a level's traffic at another size is this ratio times its
 # algorithmic bytes.  The R ratio is the one of the largest R level.
-TRAFFIC_RATIO = {"plain_c32": {"Q": 0.976, "R": 0.991, "P": 1.002},
-                 "plain_ff": {"Q": 1.001, "R": 1.003, "P": 1.001},
+TRAFFIC_RATIO = {"plain_c32": {"Q": 0.979, "R": 0.990, "P": 1.002},
+                 "plain_ff": {"Q": 1.013, "R": 1.006, "P": 1.001},
                  "mixed": {"Q": 0.975, "R": 0.982, "P": 1.000}}
 TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum per level launch at 16,384 "
                   "points, as a ratio to the level's algorithmic bytes, times this level's "
