@@ -87,6 +87,9 @@ def parse():
                          "128-RHS chunks (a short, predictable launch sequence for ncu)")
     ap.add_argument("--ncu-adjoint", action="store_true",
                     help="with --ncu-case: the plain matvecs through the adjoint view")
+    ap.add_argument("--ncu-near", action="store_true",
+                    help="with --ncu-case: attach the near field first, so that the plain "
+                         "matvecs apply near + far")
     return ap.parse_args()
 
 
@@ -480,6 +483,8 @@ def run_ncu_case(args, local):
         return
     w = build_workload(args.workload, local, args.storage)
     op, n = w["op"], w["n"]
+    if args.ncu_near:
+        op.add_near(w["pts"], w["pts"], w["tree"], w["tree"], w["k"])
     view = op.adjoint() if args.ncu_adjoint else op
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
